@@ -1,0 +1,12 @@
+"""GB300-native exact leverage-score sampling from Khatri-Rao products.
+
+Drop-in replacements for the reference's Python API on this path
+(vbharadwaj-bk/fast_tensor_leverage, cpp_ext/als_module.cpp and
+cpp_ext/partition_tree.cpp), backed by sm_103a CUDA kernels behind the C ABI
+of include/ftl.h.
+"""
+from ._lib import FTLError, PREC
+from .partition_tree import PartitionTree
+from .sampler import Sampler
+
+__all__ = ["FTLError", "PREC", "PartitionTree", "Sampler"]

@@ -1,0 +1,126 @@
+"""ctypes binding of libftl_gb300.so (C ABI declared in include/ftl.h).
+
+The library is loaded from the package's in-tree _build/ folder.  There is no
+CPU fallback: if the library is missing or CUDA is unavailable, using the
+package raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libftl_gb300.so"
+
+FTL_OK = 0
+STATUS_NAMES = {
+    1: "FTL_E_ARG",
+    2: "FTL_E_OOM",
+    3: "FTL_E_CUDA",
+    4: "FTL_E_TIMEOUT",
+    5: "FTL_E_CANCELLED",
+    6: "FTL_E_UNSUPPORTED",
+}
+PREC = {"fp64": 0, "fp32": 1}
+MAX_MODES = 16
+MAX_RANK = 128
+
+
+class FTLError(RuntimeError):
+    """A libftl_gb300 call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class TreeGeom(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in (
+        "n", "F", "leaf_count", "node_count", "lfill_level", "lfill_count", "total_levels",
+        "nodes_upto_lfill", "nodes_before_lfill", "complete_level_offset")]
+
+
+class KRPPlan(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int),
+        ("R", ctypes.c_int),
+        ("J", ctypes.c_int64),
+        ("prec", ctypes.c_int),
+        ("dims", ctypes.c_int64 * MAX_MODES),
+        ("U", ctypes.c_void_p * MAX_MODES),
+        ("gram_G", ctypes.c_void_p * MAX_MODES),
+        ("eig_G", ctypes.c_void_p),
+        ("M", ctypes.c_void_p),
+        ("lambda_", ctypes.c_void_p),
+        ("pinv32", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_INT = ctypes.c_int
+_U32 = ctypes.c_uint32
+_U64 = ctypes.c_uint64
+_SZP = ctypes.POINTER(ctypes.c_size_t)
+
+SIGNATURES = {
+    "ftl_last_error": ([], ctypes.c_char_p),
+    "ftl_abi_version": ([], _INT),
+    "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),
+    "ftl_tree_bytes": ([_I64, _I64, _INT, _INT, _SZP], _INT),
+    "ftl_tree_build": ([_P, _I64, _INT, _I64, _INT, _P, _P], _INT),
+    "ftl_tree_scale": ([_P, _P, _I64, _INT, _INT, _P, _P], _INT),
+    "ftl_tree_sample": ([_P, _INT, _P, _I64, _INT, _I64, _P, _P, _P, _P, _I64, _P], _INT),
+    "ftl_krp_plan_sizes": ([_INT, _INT, _INT, _SZP, _SZP, _SZP, _SZP], _INT),
+    "ftl_krp_compute_m": ([ctypes.POINTER(KRPPlan), _U32, _P], _INT),
+    "ftl_krp_draw": ([ctypes.POINTER(KRPPlan), _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
+    "ftl_philox_uniforms": ([_P, _I64, _U64, _U64, _P], _INT),
+}
+
+
+def lib():
+    """Load libftl_gb300.so (built by fast_tensor_leverage_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -m fast_tensor_leverage_gb300.build` "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(str(LIB_PATH), mode=os.RTLD_NOW | getattr(os, "RTLD_LOCAL", 0))
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != FTL_OK:
+        msg = lib().ftl_last_error().decode(errors="replace")
+        raise FTLError(status, f"{what}: {msg}" if what else msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))
+
+
+def tree_geometry(n: int, F: int) -> TreeGeom:
+    g = TreeGeom()
+    call("ftl_tree_geometry", n, F, ctypes.byref(g))
+    return g
+
+
+def tree_bytes(n: int, F: int, R: int, prec: int) -> int:
+    out = ctypes.c_size_t()
+    call("ftl_tree_bytes", n, F, R, prec, ctypes.byref(out))
+    return out.value
+
+
+def plan_sizes(N: int, R: int, prec: int):
+    e, m, l, p = (ctypes.c_size_t() for _ in range(4))
+    call("ftl_krp_plan_sizes", N, R, prec, ctypes.byref(e), ctypes.byref(m), ctypes.byref(l), ctypes.byref(p))
+    return e.value, m.value, l.value, p.value

@@ -1,0 +1,325 @@
+// Per-draw set-up of the exact KRP sampler (EfficientKRPSampler::computeM,
+// cpp_ext/efficient_krp_sampler.hpp:90-194), on device, in FP64:
+//
+//   M[k]   = G_k(root) o M[next included mode]      suffix Hadamard products
+//   M[0]   = full product over the included modes   (M[1] when j == 0)
+//   pinv   = sum_{lambda_v > 1e-8} v v^T / lambda_v  (eigendecomposition of M[0])
+//   M[N]   = rows lambda_v^{-1/2} v^T, descending lambda (the reference's
+//            reversed, transposed V Lambda^{-1/2})
+//   M[k]  o= pinv, then rows sqrt(lambda_v) v^T of its eigendecomposition,
+//            ascending lambda (k = 1..N-1, k != j)
+//   eigen tree k: leaves w_u w_u^T over the rows w_u of M[offset(k)],
+//            internal nodes = child sums, every node then o G_k(root).
+//
+// The eigensolver is a cyclic parallel-order (round-robin) two-sided Jacobi
+// method on a dense symmetric matrix in shared memory, one CTA per matrix,
+// rotations skipped when |a_pq| <= 2^-53 sqrt(|a_pp a_qq|) (the relative
+// criterion of Demmel and Veselic), eigenpairs sorted ascending as LAPACK's
+// dsyev returns them.  Eigenvector signs are irrelevant downstream (only
+// outer products v v^T are used).
+#include <algorithm>
+
+#include "ftl_common.cuh"
+
+namespace ftl {
+
+struct CMParams {
+    int N, R, P, prec;
+    uint32_t j;               // normalised: j < N excluded, j == N+1 none
+    const void *root[FTL_MAX_MODES];  // packed root Gram of each tree (tree precision)
+    double *M;                // (N+2) x R x R, then (N+1) x R x R Jacobi scratch
+    bool v_global;            // eigenvectors kept in the scratch slots (large R)
+    double *lambda;           // (N+1) x R
+    float *pinv32;            // P
+    void *eig_G;              // N x (2R-1) x P
+    DGeom eig;                // geometry of an eigen tree (n = R, F = 1)
+};
+
+__device__ __forceinline__ double root_at(const CMParams &p, int k, int e) {
+    if (p.prec == FTL_PREC_FP64) return ((const double *)p.root[k])[e];
+    return (double)((const float *)p.root[k])[e];
+}
+
+// In-place Jacobi on A (R x R, symmetric, row-major); V receives the
+// eigenvectors as columns; lam_rank[v] gets the ascending rank of eigenvalue v.
+// All threads of the block must call it.
+__device__ void jacobi_eigen(double *A, double *V, int R, double *csbuf, int *pqbuf, int *flag) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int n = R + (R & 1);
+    const int half = n / 2;
+    for (int e = tid; e < R * R; e += nth) V[e] = (e / R == e % R) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        if (tid == 0) *flag = 0;
+        __syncthreads();
+        for (int round = 0; round < n - 1; ++round) {
+            if (tid < half) {
+                int p, q;
+                if (tid == 0) {
+                    p = round;
+                    q = n - 1;
+                } else {
+                    p = (round + tid) % (n - 1);
+                    q = (round - tid + (n - 1)) % (n - 1);
+                }
+                if (p > q) {
+                    int t = p;
+                    p = q;
+                    q = t;
+                }
+                double c = 1.0, s = 0.0;
+                if (q < R) {
+                    double apq = A[p * R + q];
+                    double app = A[p * R + p];
+                    double aqq = A[q * R + q];
+                    if (apq != 0.0 && fabs(apq) > 1.1102230246251565e-16 * sqrt(fabs(app * aqq))) {
+                        double theta = (aqq - app) / (2.0 * apq);
+                        double t;
+                        if (fabs(theta) > 1e150)
+                            t = 0.5 / theta;
+                        else
+                            t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
+                        c = 1.0 / sqrt(1.0 + t * t);
+                        s = t * c;
+                        *flag = 1;
+                    }
+                }
+                csbuf[2 * tid] = c;
+                csbuf[2 * tid + 1] = s;
+                pqbuf[2 * tid] = p;
+                pqbuf[2 * tid + 1] = q;
+            }
+            __syncthreads();
+            // A <- A J and V <- V J (columns p, q of each rotated pair)
+            for (int w = tid; w < half * R; w += nth) {
+                int i = w / R, r = w - i * R;
+                double s = csbuf[2 * i + 1];
+                if (s == 0.0) continue;
+                double c = csbuf[2 * i];
+                int p = pqbuf[2 * i], q = pqbuf[2 * i + 1];
+                double arp = A[r * R + p], arq = A[r * R + q];
+                A[r * R + p] = c * arp - s * arq;
+                A[r * R + q] = s * arp + c * arq;
+                double vrp = V[r * R + p], vrq = V[r * R + q];
+                V[r * R + p] = c * vrp - s * vrq;
+                V[r * R + q] = s * vrp + c * vrq;
+            }
+            __syncthreads();
+            // A <- J^T A (rows p, q)
+            for (int w = tid; w < half * R; w += nth) {
+                int i = w / R, col = w - i * R;
+                double s = csbuf[2 * i + 1];
+                if (s == 0.0) continue;
+                double c = csbuf[2 * i];
+                int p = pqbuf[2 * i], q = pqbuf[2 * i + 1];
+                double apc = A[p * R + col], aqc = A[q * R + col];
+                A[p * R + col] = c * apc - s * aqc;
+                A[q * R + col] = s * apc + c * aqc;
+            }
+            __syncthreads();
+            if (tid < half) {
+                double s = csbuf[2 * tid + 1];
+                if (s != 0.0) {
+                    int p = pqbuf[2 * tid], q = pqbuf[2 * tid + 1];
+                    A[p * R + q] = 0.0;
+                    A[q * R + p] = 0.0;
+                }
+            }
+            __syncthreads();
+        }
+        if (*flag == 0) break;
+        __syncthreads();
+    }
+    __syncthreads();
+}
+
+// order[r] = index of the r-th smallest eigenvalue (ties by index).
+__device__ void sort_ascending(const double *A, int R, int *order) {
+    for (int v = threadIdx.x; v < R; v += blockDim.x) {
+        double lv = A[v * R + v];
+        int rank = 0;
+        for (int u = 0; u < R; ++u) {
+            double lu = A[u * R + u];
+            if (lu < lv || (lu == lv && u < v)) ++rank;
+        }
+        order[rank] = v;
+    }
+    __syncthreads();
+}
+
+// Shared memory: A (R*R), V (R*R unless kept in global scratch), cs (R+2),
+// pq (R+2 ints), order (R ints), flag.
+static size_t cm_smem_bytes(int R, bool v_global) {
+    return (size_t)((v_global ? 1 : 2) * R * R + R + 2) * sizeof(double) +
+           (size_t)(2 * R + 4) * sizeof(int) + 16;
+}
+
+__global__ void computem_pinv_kernel(CMParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int R = p.R, RR = R * R, N = p.N, tid = threadIdx.x, nth = blockDim.x;
+    double *A = (double *)smem_raw;
+    double *V = p.v_global ? p.M + (size_t)(N + 2) * RR : A + RR;
+    double *cs = A + (p.v_global ? 1 : 2) * RR;
+    int *pq = (int *)(cs + R + 2);
+    int *order = pq + R + 2;
+    int *flag = order + R;
+
+    // Suffix Hadamard products (full symmetric storage).
+    int last = N;  // slot N holds all ones in the reference
+    for (int k = N - 1; k >= 0; --k) {
+        if ((uint32_t)k == p.j) continue;
+        for (int e = tid; e < RR; e += nth) {
+            int a = e / R, b = e - a * R;
+            int lo = min(a, b), hi = max(a, b);
+            double g = root_at(p, k, packed_index(lo, hi, R));
+            double prev = (last == N) ? 1.0 : p.M[(size_t)last * RR + e];
+            p.M[(size_t)k * RR + e] = g * prev;
+        }
+        last = k;
+        __syncthreads();
+    }
+    if (p.j == 0) {
+        for (int e = tid; e < RR; e += nth) p.M[e] = p.M[(size_t)RR + e];
+        __syncthreads();
+    }
+    for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
+    __syncthreads();
+    jacobi_eigen(A, V, R, cs, pq, flag);
+    sort_ascending(A, R, order);
+    // W = M[N]: row (R-1-r) = v_r / sqrt(lambda_r) for lambda_r > 1e-8, else 0,
+    // r the ascending rank (column R-1-r of the reference's V Lambda^{-1/2}).
+    double *W = p.M + (size_t)N * RR;
+    for (int e = tid; e < RR; e += nth) {
+        int row = e / R, a = e - row * R;
+        int r = R - 1 - row;
+        int v = order[r];
+        double lam = A[v * R + v];
+        W[e] = lam > 1e-8 ? V[a * R + v] / sqrt(lam) : 0.0;
+    }
+    for (int r = tid; r < R; r += nth) p.lambda[r] = A[order[r] * R + order[r]];
+    __syncthreads();
+    // pinv = W^T W summed over W's rows in order (the reference's dsyrk over
+    // the columns of V Lambda^{-1/2}); full symmetric into slot 0, packed FP64
+    // into slot N+1, packed FP32 into pinv32.
+    for (int e = tid; e < RR; e += nth) {
+        int a = e / R, b = e - a * R;
+        int lo = min(a, b), hi = max(a, b);
+        double acc = 0.0;
+        for (int row = 0; row < R; ++row) acc += W[row * R + lo] * W[row * R + hi];
+        A[e] = acc;
+    }
+    __syncthreads();
+    double *pinv_packed = p.M + (size_t)(N + 1) * RR;
+    for (int e = tid; e < RR; e += nth) {
+        p.M[e] = A[e];
+        int a = e / R, b = e - a * R;
+        if (a <= b) {
+            int pe = packed_index(a, b, R);
+            pinv_packed[pe] = A[e];
+            p.pinv32[pe] = (float)A[e];
+        }
+    }
+    // M[k] o= pinv for k = N-1 .. 1, k != j
+    for (int k = N - 1; k >= 1; --k) {
+        if ((uint32_t)k == p.j) continue;
+        for (int e = tid; e < RR; e += nth) p.M[(size_t)k * RR + e] *= A[e];
+    }
+}
+
+template <typename T>
+__global__ void computem_eig_kernel(CMParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int R = p.R, RR = R * R, N = p.N, P = p.P, tid = threadIdx.x, nth = blockDim.x;
+    const int k = blockIdx.x;
+    if ((uint32_t)k == p.j || k >= N) return;
+    double *A = (double *)smem_raw;
+    double *V = p.v_global ? p.M + (size_t)(N + 3 + k) * RR : A + RR;
+    double *cs = A + (p.v_global ? 1 : 2) * RR;
+    int *pq = (int *)(cs + R + 2);
+    int *order = pq + R + 2;
+    int *flag = order + R;
+    const int offset = ((uint32_t)(k + 1) == p.j) ? k + 2 : k + 1;
+    double *W = p.M + (size_t)offset * RR;
+    if (offset < N) {
+        for (int e = tid; e < RR; e += nth) A[e] = W[e];
+        __syncthreads();
+        jacobi_eigen(A, V, R, cs, pq, flag);
+        sort_ascending(A, R, order);
+        // row r = sqrt(lambda_r) v_r, ascending (negative rounding noise -> 0)
+        for (int e = tid; e < RR; e += nth) {
+            int r = e / R, a = e - r * R;
+            int v = order[r];
+            double lam = A[v * R + v];
+            W[e] = sqrt(fmax(lam, 0.0)) * V[a * R + v];
+        }
+        for (int r = tid; r < R; r += nth) p.lambda[(size_t)offset * R + r] = A[order[r] * R + order[r]];
+        __syncthreads();
+    }
+    // Eigen tree over the R rows of W (F = 1): leaves, child sums, then o root.
+    T *G = (T *)p.eig_G + (size_t)k * (2 * R - 1) * P;
+    const DGeom g = p.eig;
+    const int leaf_count = R;
+    for (int e = tid; e < leaf_count * P; e += nth) {
+        int u = e / P, pe = e - u * P;
+        int a = 0, rem = pe;
+        while (rem >= R - a) {
+            rem -= R - a;
+            ++a;
+        }
+        int b = a + rem;
+        G[leaf_node(g, u) * P + pe] = (T)W[u * R + a] * (T)W[u * R + b];
+    }
+    __syncthreads();
+    int64_t start = g.nodes_upto_lfill - ((g.nodes_upto_lfill + 1) / 2);  // nodes_before_lfill
+    int64_t end = g.node_count - leaf_count;
+    while (true) {
+        for (int64_t e = tid; e < (end - start) * P; e += nth) {
+            int64_t c = start + e / P;
+            int pe = (int)(e % P);
+            G[c * P + pe] = G[(2 * c + 1) * P + pe] + G[(2 * c + 2) * P + pe];
+        }
+        __syncthreads();
+        if (start <= 0) break;
+        end = start;
+        start = (start + 1) / 2 - 1;
+    }
+    for (int64_t e = tid; e < (int64_t)(2 * R - 1) * P; e += nth) {
+        int pe = (int)(e % P);
+        G[e] = G[e] * (T)root_at(p, k, pe);
+    }
+}
+
+int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st) {
+    CMParams p;
+    p.N = plan->N;
+    p.R = plan->R;
+    p.P = packed_size(plan->R);
+    p.prec = plan->prec;
+    p.j = j_norm;
+    for (int k = 0; k < FTL_MAX_MODES; ++k) p.root[k] = k < plan->N ? plan->gram_G[k] : nullptr;
+    p.M = plan->M;
+    p.lambda = plan->lambda;
+    p.pinv32 = plan->pinv32;
+    p.eig_G = plan->eig_G;
+    p.eig = to_dgeom(make_geom(plan->R, 1));
+    p.v_global = cm_smem_bytes(plan->R, false) > 200 * 1024;
+    size_t smem = cm_smem_bytes(plan->R, p.v_global);
+    if (smem > 227 * 1024) return fail(FTL_E_UNSUPPORTED, "computeM: R=%d too large", plan->R);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(computem_pinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(computem_eig_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(computem_eig_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    computem_pinv_kernel<<<1, 512, smem, st>>>(p);
+    int rc = check_launch("computem_pinv_kernel");
+    if (rc) return rc;
+    if (plan->prec == FTL_PREC_FP64)
+        computem_eig_kernel<double><<<plan->N, 512, smem, st>>>(p);
+    else
+        computem_eig_kernel<float><<<plan->N, 512, smem, st>>>(p);
+    return check_launch("computem_eig_kernel");
+}
+
+}  // namespace ftl

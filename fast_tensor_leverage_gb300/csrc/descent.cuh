@@ -1,0 +1,276 @@
+// Warp-per-sample partition-tree descent shared by the standalone tree
+// sampler and the fused KRP draw.
+//
+// A descent for query x evaluates x^T G x against node Grams.  With the
+// packed upper triangle of G and the packed weighted outer product
+// xx_e = (2 - [a==b]) x_a x_b, the form is a plain dot product over
+// P = R(R+1)/2 values, so a warp holds xx in registers (R <= 32: 17 values
+// per lane) or in its shared-memory slot (R > 32) for the whole descent and
+// every level costs P coalesced loads, P FMAs and one warp reduction.
+//
+// Two arithmetics:
+//   * FP64 (parity mode): exactly the reference's decisions,
+//     cpp_ext/partition_tree.hpp:253-332 -- root mass m, cutoff = low + mL/m,
+//     go left iff draw <= cutoff, then the leaf fraction (draw-low)/(high-low)
+//     and the leaf row scan of :370-398 (exclusive prefix of q_r^2 divided by
+//     the total, first j <= F-2 with frac < q[j+1], else F-1).
+//   * FP32 (mixed mode): FP32 node Grams and forms; the draw is carried as an
+//     absolute mass offset t = (draw - low) * m in double-float (two floats),
+//     so "draw <= low + mL/m" becomes "t <= mL" and a right turn is t -= mL.
+//     Identical decisions in exact arithmetic, no FP64 instructions per level.
+#pragma once
+
+#include "ftl_common.cuh"
+
+namespace ftl {
+
+template <int RMAX>
+struct Shape {
+    static constexpr int PMAX = RMAX * (RMAX + 1) / 2;
+    static constexpr int VPL = (PMAX + 31) / 32;  // packed values per lane
+    static constexpr int XPL = (RMAX + 31) / 32;  // vector entries per lane
+    static constexpr int FQ = (RMAX + 31) / 32;   // leaf rows per lane (F <= R)
+    static constexpr bool XX_SMEM = RMAX > 32;
+    static constexpr int WARPS = RMAX <= 32 ? 8 : (RMAX <= 64 ? 4 : 2);
+};
+
+// Per-warp shared-memory slot: the query in FP64 and in the compute type,
+// plus the packed outer product when it does not fit in registers.
+template <int RMAX, typename T>
+struct WarpSlot {
+    static constexpr size_t xx_elems = Shape<RMAX>::XX_SMEM ? Shape<RMAX>::PMAX : 0;
+    static constexpr size_t bytes =
+        ((RMAX * sizeof(double) + RMAX * sizeof(T) + xx_elems * sizeof(T)) + 15) / 16 * 16;
+};
+
+template <int RMAX, typename T>
+struct QForm {
+    using S = Shape<RMAX>;
+    T r[S::XX_SMEM ? 1 : S::VPL];
+    T *s;
+    int P;
+
+    __device__ __forceinline__ void setup(const T *x, const uint16_t *pairs, int lane) {
+        if (S::XX_SMEM) {
+            for (int e = lane; e < P; e += 32) {
+                unsigned pr = pairs[e];
+                int a = pr >> 8, b = pr & 0xff;
+                T v = x[a] * x[b];
+                if (a != b) v += v;
+                s[e] = v;
+            }
+            __syncwarp();
+        } else {
+#pragma unroll
+            for (int t = 0; t < S::VPL; ++t) {
+                int e = lane + 32 * t;
+                T v = T(0);
+                if (e < P) {
+                    unsigned pr = pairs[e];
+                    int a = pr >> 8, b = pr & 0xff;
+                    v = x[a] * x[b];
+                    if (a != b) v += v;
+                }
+                r[t] = v;
+            }
+        }
+    }
+
+    __device__ __forceinline__ T eval(const T *__restrict__ node, int lane) const {
+        T acc = T(0);
+        if (S::XX_SMEM) {
+#pragma unroll 4
+            for (int e = lane; e < P; e += 32) acc = fma(__ldg(node + e), s[e], acc);
+        } else {
+#pragma unroll
+            for (int t = 0; t < S::VPL; ++t) {
+                int e = lane + 32 * t;
+                if (e < P) acc = fma(__ldg(node + e), r[t], acc);
+            }
+        }
+        return warp_sum(acc);
+    }
+};
+
+// ----------------------------------------------------------------- FP64
+
+template <int RMAX>
+__device__ __forceinline__ int64_t descend(const double *__restrict__ G, int P, const DGeom &g,
+                                           double draw, const QForm<RMAX, double> &qf, int lane,
+                                           double &frac) {
+    int64_t c = 0;
+    double low = 0.0, high = 1.0;
+    const double m = qf.eval(G, lane);
+    for (int64_t lvl = 0; lvl < g.lfill_level; ++lvl) {
+        double mL = qf.eval(G + (2 * c + 1) * (int64_t)P, lane);
+        double cutoff = low + mL / m;
+        if (draw <= cutoff) {
+            c = 2 * c + 1;
+            high = cutoff;
+        } else {
+            c = 2 * c + 2;
+            low = cutoff;
+        }
+    }
+    if (!is_leaf(g, c)) {
+        double mL = qf.eval(G + (2 * c + 1) * (int64_t)P, lane);
+        double cutoff = low + mL / m;
+        if (draw <= cutoff) {
+            c = 2 * c + 1;
+            high = cutoff;
+        } else {
+            c = 2 * c + 2;
+            low = cutoff;
+        }
+    }
+    frac = (draw - low) / (high - low);
+    return c;
+}
+
+// ----------------------------------------------------------------- FP32
+
+// t -= m for a double-float t = (th, tl) (Knuth TwoSum, then renormalise).
+__device__ __forceinline__ void df_sub(float &th, float &tl, float m) {
+    float s = th - m;
+    float bb = s - th;
+    float err = (th - (s - bb)) + (-m - bb);
+    tl += err;
+    float nh = s + tl;
+    tl = tl - (nh - s);
+    th = nh;
+}
+
+template <int RMAX>
+__device__ __forceinline__ int64_t descend(const float *__restrict__ G, int P, const DGeom &g,
+                                           double draw, const QForm<RMAX, float> &qf, int lane,
+                                           float &frac) {
+    int64_t c = 0;
+    float mP = qf.eval(G, lane);
+    double t0 = draw * (double)mP;
+    float th = (float)t0;
+    float tl = (float)(t0 - (double)th);
+    int64_t steps = g.lfill_level + 1;
+    for (int64_t lvl = 0; lvl < steps; ++lvl) {
+        if (lvl == g.lfill_level && is_leaf(g, c)) break;
+        float mL = qf.eval(G + (2 * c + 1) * (int64_t)P, lane);
+        bool left = ((th - mL) + tl) <= 0.0f;
+        if (left) {
+            c = 2 * c + 1;
+            mP = mL;
+        } else {
+            c = 2 * c + 2;
+            df_sub(th, tl, mL);
+            mP = fmaxf(mP - mL, 0.0f);
+        }
+    }
+    float f = mP > 0.0f ? (th + tl) / mP : 0.0f;
+    frac = fminf(fmaxf(f, 0.0f), 1.0f);
+    return c;
+}
+
+// ------------------------------------------------------------- leaf scan
+
+// Row selection inside leaf block c (F > 1): q_r = U[row0+r] . x for the
+// block's rows, inclusive prefix of q_r^2 in row order, first r <= F-2 with
+// frac < prefix_r / total, else F-1.  x is the warp's query in the compute
+// type (shared memory).  A selection past the last row of a partial block
+// (only reachable when frac rounds to >= 1) is clamped to that last row.
+template <int RMAX, typename T>
+__device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R, const DGeom &g,
+                                             int64_t c, T frac, const T *x, int lane) {
+    constexpr int FQ = Shape<RMAX>::FQ;
+    const int64_t leaf = leaf_index(g, c);
+    const int F = (int)g.F;
+    const int64_t row0 = leaf * g.F;
+    const int rows = (int)min((int64_t)F, g.n - row0);
+    T q2[FQ];
+#pragma unroll
+    for (int qi = 0; qi < FQ; ++qi) {
+        int r = lane + 32 * qi;
+        T q = T(0);
+        if (r < rows) {
+            const double *u = U + (row0 + r) * (int64_t)R;
+            for (int col = 0; col < R; ++col) q = fma((T)__ldg(u + col), x[col], q);
+        }
+        q2[qi] = q * q;
+    }
+    T incl[FQ];
+    T run = T(0);
+#pragma unroll
+    for (int qi = 0; qi < FQ; ++qi) incl[qi] = T(0);
+    // Sequential prefix in row order (same association as the reference's
+    // running sum); every lane walks the same sequence.
+#pragma unroll
+    for (int qi = 0; qi < FQ; ++qi) {
+        for (int rr = 0; rr < 32; ++rr) {
+            if (32 * qi + rr >= F) break;
+            T v = __shfl_sync(0xffffffffu, q2[qi], rr);
+            run += v;
+            if (lane == rr) incl[qi] = run;
+        }
+    }
+    const T tot = run;
+    int res = F - 1;
+#pragma unroll
+    for (int qi = FQ - 1; qi >= 0; --qi) {
+        int r = lane + 32 * qi;
+        bool pred;
+        if (sizeof(T) == 8)
+            pred = (r <= F - 2) && (frac < incl[qi] / tot);
+        else
+            pred = (r <= F - 2) && (frac * tot < incl[qi]);
+        unsigned bal = __ballot_sync(0xffffffffu, pred);
+        if (bal) res = 32 * qi + (__ffs(bal) - 1);
+    }
+    if (res >= rows) res = rows - 1;
+    return row0 + res;
+}
+
+// Packed (a << 8 | b) table of the upper triangle in row-major order.
+__device__ __forceinline__ void build_pairs(uint16_t *pairs, int R) {
+    const int P = packed_size(R);
+    for (int e = threadIdx.x; e < P; e += blockDim.x) {
+        int a = 0, rem = e;
+        while (rem >= R - a) {
+            rem -= R - a;
+            ++a;
+        }
+        pairs[e] = (uint16_t)((a << 8) | (a + rem));
+    }
+}
+
+// Stage an FP64 vector held as XPL entries per lane into the warp's slot:
+// xd gets it verbatim; for FP32 mode xf gets it times a power of two that
+// puts max|x| in [0.5, 1) (exact, so quadratic-form ratios are unchanged).
+// Returns that power of two (1.0 in FP64 mode).
+template <int RMAX, typename T>
+__device__ __forceinline__ double stage_query(const double (&v)[Shape<RMAX>::XPL], int R, double *xd,
+                                              T *xT, int lane) {
+    constexpr int XPL = Shape<RMAX>::XPL;
+#pragma unroll
+    for (int q = 0; q < XPL; ++q) {
+        int col = lane + 32 * q;
+        if (col < R) xd[col] = v[q];
+    }
+    double scale = 1.0;
+    if (sizeof(T) == 4) {
+        unsigned emax = 0;
+#pragma unroll
+        for (int q = 0; q < XPL; ++q) {
+            int col = lane + 32 * q;
+            unsigned e = col < R ? ((unsigned)__double2hiint(v[q]) >> 20) & 0x7ffu : 0u;
+            emax = max(emax, e);
+        }
+        emax = __reduce_max_sync(0xffffffffu, emax);
+        if (emax >= 1 && emax <= 2045) scale = __hiloint2double((int)((2046u - emax) << 20), 0);
+#pragma unroll
+        for (int q = 0; q < XPL; ++q) {
+            int col = lane + 32 * q;
+            if (col < R) xT[col] = (T)(v[q] * scale);
+        }
+    }
+    __syncwarp();
+    return scale;
+}
+
+}  // namespace ftl

@@ -1,0 +1,136 @@
+// Shared device/host helpers of libftl_gb300: status reporting, tree
+// geometry, packed-triangle indexing, warp reductions, Philox4x32-10.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/ftl.h"
+
+namespace ftl {
+
+// ------------------------------------------------------------ error state
+
+void set_error(const char *fmt, ...);
+int fail(int status, const char *fmt, ...);
+int check_launch(const char *what);
+
+#define FTL_CHECK_ARG(cond, ...)                                  \
+    do {                                                          \
+        if (!(cond)) return ::ftl::fail(FTL_E_ARG, __VA_ARGS__);  \
+    } while (0)
+
+// ---------------------------------------------------------- tree geometry
+
+// Geometry of a PartitionTree over n rows with F rows per leaf.  Mirrors the
+// constructor in cpp_ext/partition_tree.hpp:83-105: leaf_count = ceil(n/F),
+// node_count = 2*leaf_count-1, lfill_level = floor(log2(leaf_count)), the
+// partial deepest level holding leaves 0 .. (node_count-nodes_upto_lfill)-1.
+struct Geom {
+    int64_t n, F, leaf_count, node_count, lfill_level, lfill_count, total_levels,
+        nodes_upto_lfill, nodes_before_lfill, complete_level_offset;
+};
+
+inline Geom make_geom(int64_t n, int64_t F) {
+    Geom g;
+    g.n = n;
+    g.F = F;
+    g.leaf_count = (n + F - 1) / F;
+    g.node_count = 2 * g.leaf_count - 1;
+    g.lfill_level = 0;
+    g.lfill_count = 1;
+    while (g.lfill_count * 2 <= g.leaf_count) {
+        g.lfill_level++;
+        g.lfill_count *= 2;
+    }
+    g.total_levels = g.node_count > g.lfill_count ? g.lfill_level + 1 : g.lfill_level;
+    g.nodes_upto_lfill = g.lfill_count * 2 - 1;
+    g.nodes_before_lfill = g.lfill_count - 1;
+    int64_t half_partial = (g.node_count - g.nodes_upto_lfill) / 2;
+    g.complete_level_offset = g.nodes_before_lfill - half_partial;
+    return g;
+}
+
+// Compact copy used inside kernels.
+struct DGeom {
+    int64_t n, F, node_count, lfill_level, nodes_upto_lfill, complete_level_offset;
+};
+
+inline DGeom to_dgeom(const Geom &g) {
+    DGeom d;
+    d.n = g.n;
+    d.F = g.F;
+    d.node_count = g.node_count;
+    d.lfill_level = g.lfill_level;
+    d.nodes_upto_lfill = g.nodes_upto_lfill;
+    d.complete_level_offset = g.complete_level_offset;
+    return d;
+}
+
+__host__ __device__ inline bool is_leaf(const DGeom &g, int64_t c) {
+    return 2 * c + 1 >= g.node_count;
+}
+
+__host__ __device__ inline int64_t leaf_index(const DGeom &g, int64_t c) {
+    return c >= g.nodes_upto_lfill ? c - g.nodes_upto_lfill : c - g.complete_level_offset;
+}
+
+// Heap position of leaf block `leaf` (inverse of leaf_index).
+__host__ __device__ inline int64_t leaf_node(const DGeom &g, int64_t leaf) {
+    int64_t partial = g.node_count - g.nodes_upto_lfill;  // leaves on deepest level
+    return leaf < partial ? g.nodes_upto_lfill + leaf : leaf + g.complete_level_offset;
+}
+
+// ------------------------------------------------------ packed triangles
+
+__host__ __device__ inline int packed_size(int R) { return R * (R + 1) / 2; }
+__host__ __device__ inline int packed_row_offset(int a, int R) { return a * R - a * (a - 1) / 2; }
+__host__ __device__ inline int packed_index(int a, int b, int R) {
+    return packed_row_offset(a, R) + (b - a);
+}
+
+// ------------------------------------------------------------------ warps
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// --------------------------------------------------------- Philox4x32-10
+// Counter-based generator of Salmon, Moraes, Dror and Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3" (SC'11), 10 rounds, 4x32-bit counter and
+// 2x32-bit key.  Uniform #idx of a stream = the first two output words of
+// block (counter = ctr + idx) combined into a 53-bit double in [0, 1).
+
+__host__ __device__ inline void philox_round(uint32_t c[4], uint32_t k[2]) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    uint64_t p0 = (uint64_t)M0 * c[0];
+    uint64_t p1 = (uint64_t)M1 * c[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c[1] ^ k[0];
+    uint32_t n2 = hi0 ^ c[3] ^ k[1];
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+}
+
+__host__ __device__ inline double philox_uniform(uint64_t seed, uint64_t counter) {
+    uint32_t c[4] = {(uint32_t)counter, (uint32_t)(counter >> 32), 0u, 0u};
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        philox_round(c, k);
+        k[0] += W0;
+        k[1] += W1;
+    }
+    uint64_t bits = ((uint64_t)(c[0] >> 5) << 26) | (uint64_t)(c[1] >> 6);
+    return (double)bits * (1.0 / 9007199254740992.0);  // 2^-53
+}
+
+}  // namespace ftl

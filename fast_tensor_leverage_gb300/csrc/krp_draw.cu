@@ -1,0 +1,360 @@
+// Fused KRP leverage-score draw and the standalone tree sampler.
+//
+// krp_draw_kernel: one warp per sample runs, for every included mode k in
+// increasing order, the eigen-component descent (query h) and the Gram-tree
+// descent (query h o W[u]) of EfficientKRPSampler::KRPDrawSamples
+// (cpp_ext/efficient_krp_sampler.hpp:209-254), keeping the running KRP row h
+// in registers across modes, then the weight epilogue w = R / (J h^T pinv h)
+// (compute_DAGAT, cpp_ext/sampler.hpp:94-123; :257-267).  Uniforms come from
+// the caller (2N x J, the reference's layout) or from Philox4x32-10 keyed by
+// (seed, ctr + flat index) -- the same flat index, so both sources are
+// interchangeable.
+#include <algorithm>
+
+#include "descent.cuh"
+
+namespace ftl {
+
+int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st);
+int num_sms();
+
+struct DrawParams {
+    int N, R, P;
+    uint32_t j;
+    int64_t J;
+    DGeom gram[FTL_MAX_MODES];
+    DGeom eig;
+    const double *U[FTL_MAX_MODES];
+    const void *gram_G[FTL_MAX_MODES];
+    const void *eig_G;
+    const double *M;
+    const float *pinv32;
+    int offset[FTL_MAX_MODES];
+    uint64_t *samples;
+    double *h;
+    double *weights;
+    const double *draws;
+    uint64_t seed, ctr;
+};
+
+__device__ __forceinline__ double get_draw(const DrawParams &p, int64_t idx) {
+    return p.draws ? p.draws[idx] : philox_uniform(p.seed, p.ctr + (uint64_t)idx);
+}
+
+template <int RMAX, typename T>
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_draw_kernel(DrawParams p) {
+    using S = Shape<RMAX>;
+    constexpr int XPL = S::XPL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint16_t *pairs = (uint16_t *)smem_raw;
+    const int R = p.R, P = p.P;
+    build_pairs(pairs, R);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *slot =
+        smem_raw + ((S::PMAX * sizeof(uint16_t) + 15) / 16 * 16) + warp * WarpSlot<RMAX, T>::bytes;
+    double *xd = (double *)slot;
+    T *xT = sizeof(T) == 8 ? (T *)xd : (T *)(xd + RMAX);
+    QForm<RMAX, T> qf;
+    qf.P = P;
+    qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
+    const size_t RR = (size_t)R * R;
+    const size_t eig_stride = (size_t)(2 * R - 1) * P;
+
+    for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
+         i += (int64_t)gridDim.x * S::WARPS) {
+        double h[XPL];
+#pragma unroll
+        for (int q = 0; q < XPL; ++q) h[q] = 1.0;
+        for (int k = 0; k < p.N; ++k) {
+            if ((uint32_t)k == p.j) continue;
+            // eigen-component descent, query h
+            stage_query<RMAX, T>(h, R, xd, xT, lane);
+            qf.setup(xT, pairs, lane);
+            T frac;
+            int64_t c = descend<RMAX>((const T *)p.eig_G + k * eig_stride, P, p.eig,
+                                      get_draw(p, (int64_t)k * p.J + i), qf, lane, frac);
+            int64_t u = leaf_index(p.eig, c);
+            const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)u * R;
+            double xs[XPL];
+#pragma unroll
+            for (int q = 0; q < XPL; ++q) {
+                int col = lane + 32 * q;
+                xs[q] = col < R ? h[q] * Wr[col] : 0.0;
+            }
+            // Gram-tree descent, query h o W[u]
+            __syncwarp();
+            stage_query<RMAX, T>(xs, R, xd, xT, lane);
+            qf.setup(xT, pairs, lane);
+            const DGeom &g = p.gram[k];
+            c = descend<RMAX>((const T *)p.gram_G[k], P, g,
+                              get_draw(p, (int64_t)(p.N + k) * p.J + i), qf, lane, frac);
+            int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(p.U[k], R, g, c, frac, xT, lane)
+                                : leaf_index(g, c);
+            const double *Ur = p.U[k] + t * R;
+#pragma unroll
+            for (int q = 0; q < XPL; ++q) {
+                int col = lane + 32 * q;
+                if (col < R) h[q] *= Ur[col];
+            }
+            if (lane == 0) p.samples[(int64_t)k * p.J + i] = (uint64_t)t;
+            __syncwarp();
+        }
+        if (p.weights) {
+            double scale = stage_query<RMAX, T>(h, R, xd, xT, lane);
+            qf.setup(xT, pairs, lane);
+            double lev;
+            if (sizeof(T) == 8) {
+                lev = (double)qf.eval((const T *)(p.M + (size_t)(p.N + 1) * RR), lane);
+            } else {
+                lev = (double)qf.eval((const T *)p.pinv32, lane) / (scale * scale);
+            }
+            if (lane == 0) p.weights[i] = (double)R / (lev * (double)p.J);
+        }
+        if (p.h) {
+#pragma unroll
+            for (int q = 0; q < XPL; ++q) {
+                int col = lane + 32 * q;
+                if (col < R) p.h[i * R + col] = h[q];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+struct TreeSampleParams {
+    const void *G;
+    const double *U;
+    int R, P;
+    DGeom g;
+    double *h;
+    const double *scaled_h;
+    uint64_t *samples;
+    const double *draws;
+    int64_t J;
+};
+
+// PartitionTree::PTSample_internal (cpp_ext/partition_tree.hpp:232-405):
+// x = scaled_h[i]; samples[i] = selected row; h[i] o= U[row].
+template <int RMAX, typename T>
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) tree_sample_kernel(TreeSampleParams p) {
+    using S = Shape<RMAX>;
+    constexpr int XPL = S::XPL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint16_t *pairs = (uint16_t *)smem_raw;
+    const int R = p.R, P = p.P;
+    build_pairs(pairs, R);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *slot =
+        smem_raw + ((S::PMAX * sizeof(uint16_t) + 15) / 16 * 16) + warp * WarpSlot<RMAX, T>::bytes;
+    double *xd = (double *)slot;
+    T *xT = sizeof(T) == 8 ? (T *)xd : (T *)(xd + RMAX);
+    QForm<RMAX, T> qf;
+    qf.P = P;
+    qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
+    for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
+         i += (int64_t)gridDim.x * S::WARPS) {
+        double x[XPL];
+#pragma unroll
+        for (int q = 0; q < XPL; ++q) {
+            int col = lane + 32 * q;
+            x[q] = col < R ? p.scaled_h[i * R + col] : 0.0;
+        }
+        stage_query<RMAX, T>(x, R, xd, xT, lane);
+        qf.setup(xT, pairs, lane);
+        T frac;
+        int64_t c = descend<RMAX>((const T *)p.G, P, p.g, p.draws[i], qf, lane, frac);
+        int64_t t = p.g.F > 1 ? leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, xT, lane)
+                              : leaf_index(p.g, c);
+        if (lane == 0) p.samples[i] = (uint64_t)t;
+#pragma unroll
+        for (int q = 0; q < XPL; ++q) {
+            int col = lane + 32 * q;
+            if (col < R) p.h[i * R + col] *= p.U[t * R + col];
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void philox_fill_kernel(double *out, int64_t n, uint64_t seed, uint64_t ctr) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = philox_uniform(seed, ctr + (uint64_t)i);
+}
+
+template <int RMAX, typename T>
+static size_t desc_smem() {
+    return (Shape<RMAX>::PMAX * sizeof(uint16_t) + 15) / 16 * 16 +
+           (size_t)Shape<RMAX>::WARPS * WarpSlot<RMAX, T>::bytes;
+}
+
+template <int RMAX, typename T>
+static int launch_draw(const DrawParams &p, cudaStream_t st) {
+    const int warps = Shape<RMAX>::WARPS;
+    size_t smem = desc_smem<RMAX, T>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(krp_draw_kernel<RMAX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::max<size_t>(smem, 48 * 1024));
+        attr = true;
+    }
+    int64_t blocks = (p.J + warps - 1) / warps;
+    blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
+    krp_draw_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
+    return check_launch("krp_draw_kernel");
+}
+
+template <int RMAX, typename T>
+static int launch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
+    const int warps = Shape<RMAX>::WARPS;
+    size_t smem = desc_smem<RMAX, T>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(tree_sample_kernel<RMAX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::max<size_t>(smem, 48 * 1024));
+        attr = true;
+    }
+    int64_t blocks = (p.J + warps - 1) / warps;
+    blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
+    tree_sample_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
+    return check_launch("tree_sample_kernel");
+}
+
+template <typename T>
+static int dispatch_draw(const DrawParams &p, cudaStream_t st) {
+    if (p.R <= 32) return launch_draw<32, T>(p, st);
+    if (p.R <= 64) return launch_draw<64, T>(p, st);
+    return launch_draw<128, T>(p, st);
+}
+
+// The register/shared-memory shapes are chosen by max(R, F): a lane handles
+// RMAX/32 vector entries and RMAX/32 rows of a leaf block.
+template <typename T>
+static int dispatch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
+    const int64_t RF = std::max<int64_t>(p.R, p.g.F);
+    if (RF <= 32) return launch_tree_sample<32, T>(p, st);
+    if (RF <= 64) return launch_tree_sample<64, T>(p, st);
+    return launch_tree_sample<128, T>(p, st);
+}
+
+static int validate_plan(const ftl_krp_plan *plan) {
+    FTL_CHECK_ARG(plan != nullptr, "krp: plan is NULL");
+    FTL_CHECK_ARG(plan->N >= 1 && plan->N <= FTL_MAX_MODES, "krp: N=%d outside [1, %d]", plan->N,
+                  FTL_MAX_MODES);
+    FTL_CHECK_ARG(plan->R >= 1 && plan->R <= FTL_MAX_RANK, "krp: R=%d outside [1, %d]", plan->R,
+                  FTL_MAX_RANK);
+    FTL_CHECK_ARG(plan->J >= 1, "krp: J=%lld must be positive", (long long)plan->J);
+    FTL_CHECK_ARG(plan->prec == FTL_PREC_FP64 || plan->prec == FTL_PREC_FP32, "krp: bad precision %d",
+                  plan->prec);
+    FTL_CHECK_ARG(plan->eig_G && plan->M && plan->lambda && plan->pinv32, "krp: null workspace pointer");
+    for (int k = 0; k < plan->N; ++k) {
+        FTL_CHECK_ARG(plan->dims[k] >= 1, "krp: dims[%d]=%lld must be positive", k, (long long)plan->dims[k]);
+        FTL_CHECK_ARG(plan->U[k] && plan->gram_G[k], "krp: null factor or tree pointer for mode %d", k);
+    }
+    return FTL_OK;
+}
+
+static uint32_t normalise_j(const ftl_krp_plan *plan, uint32_t j) {
+    return j < (uint32_t)plan->N ? j : (uint32_t)plan->N + 1;
+}
+
+}  // namespace ftl
+
+using namespace ftl;
+
+extern "C" int ftl_krp_plan_sizes(int N, int R, int prec, size_t *eig_bytes, size_t *M_bytes,
+                                  size_t *lambda_bytes, size_t *pinv32_bytes) {
+    FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && R >= 1 && R <= FTL_MAX_RANK,
+                  "ftl_krp_plan_sizes: bad N=%d R=%d", N, R);
+    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_krp_plan_sizes: bad precision");
+    const size_t P = (size_t)packed_size(R);
+    if (eig_bytes) *eig_bytes = (size_t)N * (2 * R - 1) * P * (prec == FTL_PREC_FP64 ? 8 : 4);
+    if (M_bytes) *M_bytes = (size_t)(2 * N + 3) * R * R * sizeof(double);
+    if (lambda_bytes) *lambda_bytes = (size_t)(N + 1) * R * sizeof(double);
+    if (pinv32_bytes) *pinv32_bytes = P * sizeof(float);
+    return FTL_OK;
+}
+
+extern "C" int ftl_krp_compute_m(const ftl_krp_plan *plan, uint32_t j, void *stream) {
+    int rc = validate_plan(plan);
+    if (rc) return rc;
+    uint32_t jn = normalise_j(plan, j);
+    int included = 0;
+    for (int k = 0; k < plan->N; ++k) included += ((uint32_t)k != jn);
+    FTL_CHECK_ARG(included >= 1, "krp: no mode left to sample (N=%d, j=%u)", plan->N, j);
+    return computem_launch(plan, jn, (cudaStream_t)stream);
+}
+
+extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
+                            double *weights, const double *draws, uint64_t seed, uint64_t ctr,
+                            void *stream) {
+    int rc = ftl_krp_compute_m(plan, j, stream);
+    if (rc) return rc;
+    FTL_CHECK_ARG(samples != nullptr, "ftl_krp_draw: samples is NULL");
+    DrawParams p;
+    p.N = plan->N;
+    p.R = plan->R;
+    p.P = packed_size(plan->R);
+    p.j = normalise_j(plan, j);
+    p.J = plan->J;
+    for (int k = 0; k < FTL_MAX_MODES; ++k) {
+        if (k < plan->N) {
+            Geom g = make_geom(plan->dims[k], std::min<int64_t>(plan->R, plan->dims[k]));
+            p.gram[k] = to_dgeom(g);
+            p.U[k] = plan->U[k];
+            p.gram_G[k] = plan->gram_G[k];
+            p.offset[k] = ((uint32_t)(k + 1) == p.j) ? k + 2 : k + 1;
+        } else {
+            p.U[k] = nullptr;
+            p.gram_G[k] = nullptr;
+            p.offset[k] = 0;
+        }
+    }
+    p.eig = to_dgeom(make_geom(plan->R, 1));
+    p.eig_G = plan->eig_G;
+    p.M = plan->M;
+    p.pinv32 = plan->pinv32;
+    p.samples = samples;
+    p.h = h;
+    p.weights = weights;
+    p.draws = draws;
+    p.seed = seed;
+    p.ctr = ctr;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (plan->prec == FTL_PREC_FP64) return dispatch_draw<double>(p, st);
+    return dispatch_draw<float>(p, st);
+}
+
+extern "C" int ftl_tree_sample(const void *G, int prec, const double *U, int64_t n, int R, int64_t F,
+                               double *h, const double *scaled_h, uint64_t *samples,
+                               const double *draws, int64_t J, void *stream) {
+    FTL_CHECK_ARG(G && U && h && scaled_h && samples && draws, "ftl_tree_sample: null pointer");
+    FTL_CHECK_ARG(n >= 1 && R >= 1 && R <= FTL_MAX_RANK && F >= 1 && F <= FTL_MAX_RANK && J >= 0,
+                  "ftl_tree_sample: bad shape n=%lld R=%d F=%lld J=%lld (need R, F in [1, %d])",
+                  (long long)n, R, (long long)F, (long long)J, FTL_MAX_RANK);
+    if (J == 0) return FTL_OK;
+    TreeSampleParams p;
+    p.G = G;
+    p.U = U;
+    p.R = R;
+    p.P = packed_size(R);
+    p.g = to_dgeom(make_geom(n, F));
+    p.h = h;
+    p.scaled_h = scaled_h;
+    p.samples = samples;
+    p.draws = draws;
+    p.J = J;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (prec == FTL_PREC_FP64) return dispatch_tree_sample<double>(p, st);
+    if (prec == FTL_PREC_FP32) return dispatch_tree_sample<float>(p, st);
+    return fail(FTL_E_ARG, "ftl_tree_sample: bad precision %d", prec);
+}
+
+extern "C" int ftl_philox_uniforms(double *out, int64_t n, uint64_t seed, uint64_t ctr, void *stream) {
+    FTL_CHECK_ARG(out != nullptr && n >= 0, "ftl_philox_uniforms: bad arguments");
+    if (n == 0) return FTL_OK;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 16);
+    philox_fill_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, n, seed, ctr);
+    return check_launch("philox_fill_kernel");
+}

@@ -1,0 +1,244 @@
+// Partition-tree construction: leaf block Grams U_blk^T U_blk and the
+// level-by-level child sums, stored as packed upper triangles in heap order.
+//
+// Semantics follow PartitionTree::build_tree (cpp_ext/partition_tree.hpp:120-170):
+// leaf block `b` covers rows [b*F, min((b+1)*F, n)), sits at heap position
+// leaf_node(b), and every internal node is the elementwise sum of its two
+// children (parent = left + right, the reference's association).
+//
+// Work layout: one CTA loads LB leaf blocks into shared memory (converted to
+// the tree precision, columns zero-padded to a multiple of 4), then each
+// thread accumulates one 4x4 tile of the upper triangle of one block's Gram
+// over the block's rows (2 vector shared loads per 16 FMAs) and writes its
+// packed elements.  The HBM traffic is the read of U plus the write of the
+// leaf Grams; the internal levels are a second, purely elementwise pass.
+#include <algorithm>
+#include <cstdio>
+
+#include "ftl_common.cuh"
+
+namespace ftl {
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    using type = float4;
+};
+template <>
+struct Vec4<double> {
+    using type = double4_32a;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict__ U, int64_t n,
+                                                        int R, int RP, DGeom g, int LB,
+                                                        T *__restrict__ G) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    T *Us = reinterpret_cast<T *>(smem_raw);  // LB x F x RP
+    const int64_t F = g.F;
+    const int P = packed_size(R);
+    const int nt = RP / 4;
+    const int tiles = nt * (nt + 1) / 2;
+    const int64_t leaf_count = (n + F - 1) / F;
+    const int64_t nbatch = (leaf_count + LB - 1) / LB;
+    const int64_t blk_elems = F * RP;
+
+    for (int64_t batch = blockIdx.x; batch < nbatch; batch += gridDim.x) {
+        const int64_t leaf0 = batch * LB;
+        // Stage LB blocks (rows past n and columns past R are zero).
+        const int64_t total = (int64_t)LB * blk_elems;
+        for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+            int64_t lb = e / blk_elems;
+            int64_t rem = e - lb * blk_elems;
+            int64_t r = rem / RP;
+            int col = (int)(rem - r * RP);
+            int64_t row = (leaf0 + lb) * F + r;
+            T v = T(0);
+            if (leaf0 + lb < leaf_count && row < n && col < R) v = (T)U[row * R + col];
+            Us[e] = v;
+        }
+        __syncthreads();
+        const int work = LB * tiles;
+        for (int w = threadIdx.x; w < work; w += blockDim.x) {
+            int lb = w / tiles;
+            int tile = w - lb * tiles;
+            int64_t leaf = leaf0 + lb;
+            if (leaf >= leaf_count) continue;
+            // tile -> (ta, tb), ta <= tb, row-major over the upper triangle
+            int ta = 0, rem = tile;
+            while (rem >= nt - ta) {
+                rem -= nt - ta;
+                ++ta;
+            }
+            int tb = ta + rem;
+            T acc[4][4];
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 4; ++y) acc[x][y] = T(0);
+            const T *base = Us + (int64_t)lb * blk_elems;
+            for (int64_t r = 0; r < F; ++r) {
+                typename Vec4<T>::type va =
+                    *reinterpret_cast<const typename Vec4<T>::type *>(base + r * RP + 4 * ta);
+                typename Vec4<T>::type vb =
+                    *reinterpret_cast<const typename Vec4<T>::type *>(base + r * RP + 4 * tb);
+                T a4[4] = {va.x, va.y, va.z, va.w};
+                T b4[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) acc[x][y] = fma(a4[x], b4[y], acc[x][y]);
+            }
+            T *Gn = G + leaf_node(g, leaf) * (int64_t)P;
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                int a = 4 * ta + x;
+                if (a >= R) continue;
+#pragma unroll
+                for (int y = 0; y < 4; ++y) {
+                    int b = 4 * tb + y;
+                    if (b < a || b >= R) continue;
+                    Gn[packed_index(a, b, R)] = acc[x][y];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// G[c] = G[2c+1] + G[2c+2] for c in [start, end).
+template <typename T>
+__global__ void level_sum_kernel(T *__restrict__ G, int64_t start, int64_t end, int P) {
+    const int64_t total = (end - start) * (int64_t)P;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = start + e / P;
+        int k = (int)(e % P);
+        G[c * P + k] = G[(2 * c + 1) * P + k] + G[(2 * c + 2) * P + k];
+    }
+}
+
+template <typename T>
+__global__ void tree_scale_kernel(const T *__restrict__ src, T *__restrict__ dst, int64_t total,
+                                  int P, const double *__restrict__ mat) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        dst[e] = (T)((double)src[e] * mat[e % P]);
+    }
+}
+
+static int sm_count() {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+        if (cached <= 0) cached = 148;
+    }
+    return cached;
+}
+
+int num_sms() { return sm_count(); }
+
+template <typename T>
+static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaStream_t st) {
+    Geom geom = make_geom(n, F);
+    DGeom g = to_dgeom(geom);
+    const int P = packed_size(R);
+    const int RP = (R + 3) / 4 * 4;
+    const size_t blk_bytes = (size_t)F * RP * sizeof(T);
+    const int nt = RP / 4;
+    const int tiles = nt * (nt + 1) / 2;
+    // Leaves per CTA: fill the 256 threads with 4x4 tiles, bounded by shared memory.
+    int LB = std::max(1, 256 / tiles);
+    while (LB > 1 && (size_t)LB * blk_bytes > 112u * 1024u) --LB;
+    size_t smem = (size_t)LB * blk_bytes;
+    if (smem > 48 * 1024) {
+        if (smem > 227 * 1024)
+            return fail(FTL_E_UNSUPPORTED, "tree_build: leaf block of %lld x %d needs %zu B of shared memory",
+                        (long long)F, R, smem);
+        cudaFuncSetAttribute(leaf_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    int64_t nbatch = (geom.leaf_count + LB - 1) / LB;
+    int grid = (int)std::min<int64_t>(nbatch, (int64_t)sm_count() * 8);
+    leaf_gram_kernel<T><<<grid, 256, smem, st>>>(U, n, R, RP, g, LB, G);
+    int rc = check_launch("leaf_gram_kernel");
+    if (rc) return rc;
+    int64_t start = geom.nodes_before_lfill;
+    int64_t end = geom.node_count - geom.leaf_count;
+    while (true) {
+        if (end > start) {
+            int64_t total = (end - start) * (int64_t)P;
+            int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+            level_sum_kernel<T><<<blocks, 256, 0, st>>>(G, start, end, P);
+            rc = check_launch("level_sum_kernel");
+            if (rc) return rc;
+        }
+        if (start <= 0) break;
+        end = start;
+        start = (start + 1) / 2 - 1;
+    }
+    return FTL_OK;
+}
+
+}  // namespace ftl
+
+using namespace ftl;
+
+extern "C" int ftl_tree_geometry(int64_t n, int64_t F, ftl_tree_geom *out) {
+    FTL_CHECK_ARG(out != nullptr, "ftl_tree_geometry: out is NULL");
+    FTL_CHECK_ARG(n >= 1 && F >= 1, "ftl_tree_geometry: need n >= 1 and F >= 1 (got n=%lld F=%lld)",
+                  (long long)n, (long long)F);
+    Geom g = make_geom(n, F);
+    out->n = g.n;
+    out->F = g.F;
+    out->leaf_count = g.leaf_count;
+    out->node_count = g.node_count;
+    out->lfill_level = g.lfill_level;
+    out->lfill_count = g.lfill_count;
+    out->total_levels = g.total_levels;
+    out->nodes_upto_lfill = g.nodes_upto_lfill;
+    out->nodes_before_lfill = g.nodes_before_lfill;
+    out->complete_level_offset = g.complete_level_offset;
+    return FTL_OK;
+}
+
+extern "C" int ftl_tree_bytes(int64_t n, int64_t F, int R, int prec, size_t *out_bytes) {
+    FTL_CHECK_ARG(out_bytes != nullptr, "ftl_tree_bytes: out_bytes is NULL");
+    FTL_CHECK_ARG(n >= 1 && F >= 1 && R >= 1 && R <= FTL_MAX_RANK,
+                  "ftl_tree_bytes: bad shape n=%lld F=%lld R=%d", (long long)n, (long long)F, R);
+    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_tree_bytes: bad precision %d", prec);
+    Geom g = make_geom(n, F);
+    *out_bytes = (size_t)g.node_count * packed_size(R) * (prec == FTL_PREC_FP64 ? 8 : 4);
+    return FTL_OK;
+}
+
+extern "C" int ftl_tree_build(const double *U, int64_t n, int R, int64_t F, int prec, void *G,
+                              void *stream) {
+    FTL_CHECK_ARG(U != nullptr && G != nullptr, "ftl_tree_build: null pointer");
+    FTL_CHECK_ARG(n >= 1 && F >= 1 && R >= 1 && R <= FTL_MAX_RANK,
+                  "ftl_tree_build: bad shape n=%lld F=%lld R=%d", (long long)n, (long long)F, R);
+    FTL_CHECK_ARG(F <= FTL_MAX_RANK, "ftl_tree_build: F=%lld exceeds %d", (long long)F, FTL_MAX_RANK);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (prec == FTL_PREC_FP64) return build_impl<double>(U, n, R, F, (double *)G, st);
+    if (prec == FTL_PREC_FP32) return build_impl<float>(U, n, R, F, (float *)G, st);
+    return fail(FTL_E_ARG, "ftl_tree_build: bad precision %d", prec);
+}
+
+extern "C" int ftl_tree_scale(const void *G_src, void *G_dst, int64_t node_count, int R, int prec,
+                              const double *mat, void *stream) {
+    FTL_CHECK_ARG(G_src && G_dst && mat, "ftl_tree_scale: null pointer");
+    FTL_CHECK_ARG(node_count >= 1 && R >= 1 && R <= FTL_MAX_RANK, "ftl_tree_scale: bad shape");
+    const int P = packed_size(R);
+    int64_t total = node_count * (int64_t)P;
+    int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (prec == FTL_PREC_FP64)
+        tree_scale_kernel<double><<<blocks, 256, 0, st>>>((const double *)G_src, (double *)G_dst, total, P, mat);
+    else if (prec == FTL_PREC_FP32)
+        tree_scale_kernel<float><<<blocks, 256, 0, st>>>((const float *)G_src, (float *)G_dst, total, P, mat);
+    else
+        return fail(FTL_E_ARG, "ftl_tree_scale: bad precision %d", prec);
+    return check_launch("tree_scale_kernel");
+}

@@ -1,0 +1,93 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the reference C++ sampler (vbharadwaj-bk/fast_tensor_leverage,
+cpp_ext/efficient_krp_sampler.hpp and cpp_ext/partition_tree.hpp), compiled
+from its sources by `make -C oracle ref` into oracle/_ref/ftl_ref*.so, on
+seeded inputs with injected uniforms, and stores inputs, uniforms and the
+reference's outputs (sample indices, h, weights, node Grams).
+
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parents[1]
+sys.path.insert(0, str(REPO / "oracle" / "_ref"))
+
+import ftl_ref  # noqa: E402
+
+# name: (N, dims, R, J, j, seed, heavy_rows)
+KRP_CASES = {
+    "krp_readme_shape": (4, [1000] * 4, 8, 2000, 5, 11, 0.0),
+    "krp_partial_leaf_excl1": (3, [1001, 1001, 1001], 8, 1500, 1, 12, 0.0),
+    "krp_ragged_r25_excl0": (3, [300, 1500, 64], 25, 1000, 0, 13, 0.0),
+    "krp_rows_lt_rank": (3, [20, 20, 20], 32, 800, 4, 14, 0.0),
+    "krp_r32_heavy_excl_last": (3, [1024, 512, 700], 32, 800, 2, 15, 0.01),
+}
+
+# name: (n, F, R, J, seed)
+TREE_CASES = {
+    "tree_partial_n1001_f8": (1001, 8, 8, 1000, 21),
+    "tree_complete_n1024_f32": (1024, 32, 32, 600, 22),
+    "tree_f1_n13": (13, 1, 13, 500, 23),
+}
+
+
+def make_factors(rng, dims, R, heavy):
+    U = []
+    for n in dims:
+        u = rng.normal(size=(n, R))
+        if heavy > 0:
+            rows = rng.choice(n, size=max(1, int(heavy * n)), replace=False)
+            u[rows] *= 100.0
+        U.append(u)
+    return U
+
+
+def main() -> None:
+    for name, (N, dims, R, J, j, seed, heavy) in KRP_CASES.items():
+        rng = np.random.default_rng(seed)
+        U = make_factors(rng, dims, R, heavy)
+        draws = rng.random(2 * N * J)
+        s = ftl_ref.RefSampler(U, J, R)
+        samples = np.zeros((N, J), dtype=np.uint64)
+        s.draw(j, samples, draws)
+        h = np.zeros((J, R))
+        w = np.zeros(J)
+        s.get_h(h)
+        s.get_weights(w)
+        out = {f"U{k}": U[k] for k in range(N)}
+        out.update(N=N, R=R, J=J, j=j, draws=draws, samples=samples, h=h, weights=w)
+        np.savez_compressed(HERE / f"{name}.npz", **out)
+        print(name, "written")
+    for name, (n, F, R, J, seed) in TREE_CASES.items():
+        rng = np.random.default_rng(seed)
+        U = rng.normal(size=(n, R))
+        scaled_h = rng.normal(size=(J, R))
+        h = rng.normal(size=(J, R))
+        draws = rng.random(J)
+        t = ftl_ref.RefPartitionTree(n, F, J, R)
+        t.build_tree(U)
+        geom = t.geometry()
+        G = np.zeros((geom["node_count"], R, R))
+        t.get_G(G)
+        h_out = h.copy()
+        samples = np.zeros(J, dtype=np.uint64)
+        t.PTSample(U, h_out, scaled_h, samples, draws)
+        iu = np.triu_indices(R)
+        np.savez_compressed(
+            HERE / f"{name}.npz", n=n, F=F, R=R, J=J, U=U, h=h, scaled_h=scaled_h, draws=draws,
+            G_packed=G[:, iu[0], iu[1]], samples=samples, h_out=h_out,
+            geometry=np.array([geom[k] for k in (
+                "leaf_count", "node_count", "lfill_level", "lfill_count", "total_levels",
+                "nodes_upto_lfill", "nodes_before_lfill", "complete_level_offset")], dtype=np.int64))
+        print(name, "written")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,79 @@
+"""CPU: the C-ABI library loads and exports every entry point include/ftl.h
+declares; host-only entry points (geometry, sizes, argument validation) work
+without a GPU and agree with the oracle."""
+import ctypes
+import re
+
+import numpy as np
+import pytest
+
+from fast_tensor_leverage_gb300 import _lib
+from oracle import oracle as O
+from tests.conftest import REPO
+
+
+def declared_functions():
+    text = (REPO / "include" / "ftl.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ftl_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "ftl_krp_draw" in names and "ftl_tree_build" in names and len(names) >= 10
+
+
+def test_library_exports_every_declared_symbol():
+    L = ctypes.CDLL(str(_lib.LIB_PATH))
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, f"missing exports: {missing}"
+    # and the Python binding covers all of them
+    assert set(declared_functions()) <= set(_lib.SIGNATURES), \
+        set(declared_functions()) - set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("n,F", [(1, 1), (5, 8), (8, 8), (1000, 8), (1001, 8), (520, 8),
+                                 (13, 1), (8388608, 32), (4800000, 25), (65536, 64), (777, 16)])
+def test_geometry_matches_oracle(n, F):
+    g = _lib.tree_geometry(n, F)
+    o = O.geometry(n, F)
+    for k in O.GEOM_KEYS:
+        assert getattr(g, k) == o[k], k
+
+
+def test_sizes():
+    R = 32
+    P = R * (R + 1) // 2
+    assert _lib.tree_bytes(2**23, 32, R, _lib.PREC["fp32"]) == (2 * 2**18 - 1) * P * 4
+    assert _lib.tree_bytes(1001, 8, 8, _lib.PREC["fp64"]) == (2 * 126 - 1) * 36 * 8
+    e, m, l, p = _lib.plan_sizes(3, R, _lib.PREC["fp64"])
+    assert e == 3 * (2 * R - 1) * P * 8 and l == 4 * R * 8 and p == P * 4
+    assert m >= 5 * R * R * 8
+
+
+@pytest.mark.parametrize("call", [
+    lambda: _lib.call("ftl_tree_build", None, 10, 8, 8, 0, None, None),
+    lambda: _lib.call("ftl_tree_build", 1, 10, 0, 8, 0, 1, None),
+    lambda: _lib.call("ftl_tree_build", 1, 10, 129, 8, 0, 1, None),
+    lambda: _lib.call("ftl_tree_build", 1, 10, 8, 8, 7, 1, None),
+    lambda: _lib.call("ftl_tree_sample", 1, 0, 1, 10, 8, 0, 1, 1, 1, 1, 5, None),
+    lambda: _lib.tree_geometry(0, 8),
+    lambda: _lib.plan_sizes(0, 8, 0),
+    lambda: _lib.plan_sizes(17, 8, 0),
+    lambda: _lib.call("ftl_krp_draw", None, 0, 1, None, None, None, 0, 0, None),
+])
+def test_invalid_arguments_return_ftl_e_arg(call):
+    with pytest.raises(_lib.FTLError) as ei:
+        call()
+    assert ei.value.status == 1  # FTL_E_ARG, raised before any CUDA call
+
+
+def test_plan_validation_rejects_bad_plans():
+    plan = _lib.KRPPlan()
+    plan.N, plan.R, plan.J, plan.prec = 3, 8, 100, 0
+    with pytest.raises(_lib.FTLError) as ei:  # null workspaces
+        _lib.call("ftl_krp_compute_m", ctypes.byref(plan), 0, None)
+    assert ei.value.status == 1
+    plan.N = 0
+    with pytest.raises(_lib.FTLError):
+        _lib.call("ftl_krp_compute_m", ctypes.byref(plan), 0, None)

@@ -1,0 +1,238 @@
+"""GPU parity of the exact KRP sampler and the partition tree against the
+reference's golden outputs and the CPU oracle.
+
+Tolerances:
+  * FP64 mode: sample indices bit-exact.  A sample may differ only if the
+    oracle's smallest decision margin for it (distance between a uniform and
+    a cutoff it was compared with) is below NEAR_TIE -- the quadratic forms
+    are summed in a different order than the reference's BLAS, so decisions
+    that close are rounding-dependent.  h of a matching sample is bit-exact
+    (the same rows multiplied in the same order); weights within 1e-9
+    relative (FP64 pseudo-inverse from a Jacobi eigensolver vs LAPACK).
+  * FP32 mode: index agreement with the FP64 oracle >= 99%, weights within
+    1e-3 relative, and the empirical distribution within sampling noise of
+    the exact leverage distribution (total variation).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests._golden import included_rows, krp_cases, load_krp, load_tree, tree_cases
+
+pytestmark = pytest.mark.gpu
+
+NEAR_TIE = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ftl():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fast_tensor_leverage_gb300 as m
+    return m
+
+
+def check_indices(got, want, margin, rows, max_ties_frac=1e-3):
+    mism = (got[rows] != want[rows]).any(axis=0)
+    n = int(mism.sum())
+    if n:
+        assert margin is not None, f"{n} mismatching samples"
+        assert np.all(margin[mism] < NEAR_TIE), (
+            f"{n} mismatches, margins {np.sort(margin[mism])[-5:]}")
+        assert n <= max(1, max_ties_frac * got.shape[1])
+    return mism
+
+
+@pytest.mark.parametrize("name", krp_cases())
+def test_fp64_draw_matches_reference_golden(ftl, name):
+    c = load_krp(name)
+    N, J, R, j = c["N"], c["J"], c["R"], c["j"]
+    s = ftl.Sampler(c["U"], J, R, "efficient", precision="fp64")
+    samples = np.zeros((N, J), dtype=np.uint64)
+    h = np.zeros((J, R))
+    w = np.zeros(J)
+    s.KRPDrawSamples_materialize(j, samples, h, w, draws=c["draws"])
+    o = O.OracleKRPSampler(c["U"], J, R)
+    o.draw(j, c["draws"], want_margin=True)
+    rows = included_rows(N, j)
+    mism = check_indices(samples, c["samples"], o.margin, rows)
+    ok = ~mism
+    assert np.array_equal(h[ok], c["h"][ok])
+    np.testing.assert_allclose(w[ok], c["weights"][ok], rtol=1e-9)
+    # row j is left untouched when a mode is excluded
+    if j < N:
+        assert not samples[j].any()
+
+
+@pytest.mark.parametrize("N,dims,R,J,j,seed", [
+    (4, [1000] * 4, 8, 10000, 5, 101),       # README shape, none excluded
+    (3, [1001] * 3, 8, 5000, 1, 102),        # partial leaf, mode excluded
+    (3, [2048, 777, 4096], 32, 4000, 0, 103),
+    (3, [300, 1500, 64], 25, 3000, 2, 104),  # R not a power of two, F = R
+    (2, [5000, 3000], 64, 2000, 3, 105),     # R > 32: shared-memory forms
+    (2, [600, 700], 128, 600, 3, 106),       # R = 128: eigenvectors in scratch
+    (3, [20, 30, 40], 32, 1500, 4, 107),     # I < R: F = I, single-leaf trees
+    (6, [50, 60, 70, 80, 90, 100], 16, 2000, 3, 108),
+])
+def test_fp64_draw_matches_oracle(ftl, N, dims, R, J, j, seed):
+    rng = np.random.default_rng(seed)
+    U = [rng.normal(size=(n, R)) for n in dims]
+    rows_heavy = rng.choice(dims[0], size=max(1, dims[0] // 100), replace=False)
+    U[0][rows_heavy] *= 100.0
+    draws = rng.random(2 * N * J)
+    s = ftl.Sampler(U, J, R, "efficient", precision="fp64")
+    samples = np.zeros((N, J), dtype=np.uint64)
+    h = np.zeros((J, R))
+    w = np.zeros(J)
+    s.KRPDrawSamples_materialize(j, samples, h, w, draws=draws)
+    o = O.OracleKRPSampler(U, J, R)
+    ref = o.draw(j, draws, want_margin=True)
+    rows = included_rows(N, j if j < N else N + 1)
+    mism = check_indices(samples, ref, o.margin, rows)
+    ok = ~mism
+    assert np.array_equal(h[ok], o.h[ok])
+    np.testing.assert_allclose(w[ok], o.weights[ok], rtol=1e-9)
+
+
+def test_philox_stream_equals_injected_oracle_uniforms(ftl):
+    rng = np.random.default_rng(7)
+    N, I, R, J = 4, 1000, 8, 10000
+    U = [rng.normal(size=(I, R)) for _ in range(N)]
+    seed = 0x1234_5678_9ABC
+    s = ftl.Sampler(U, J, R, "efficient", precision="fp64", seed=seed)
+    dev = torch.empty(2 * N * J, dtype=torch.float64, device="cuda")
+    from fast_tensor_leverage_gb300 import _lib
+    _lib.call("ftl_philox_uniforms", dev.data_ptr(), dev.numel(), seed, 0,
+              torch.cuda.current_stream().cuda_stream)
+    uni = O.philox_uniforms(seed, 0, 2 * N * J)
+    assert np.array_equal(dev.cpu().numpy(), uni)
+    samples = np.zeros((N, J), dtype=np.uint64)
+    s.KRPDrawSamples(N + 1, samples)  # in-kernel Philox, counter 0
+    o = O.OracleKRPSampler(U, J, R)
+    ref = o.draw(N + 1, uni, want_margin=True)
+    check_indices(samples, ref, o.margin, list(range(N)))
+    # the next call continues the stream
+    samples2 = np.zeros((N, J), dtype=np.uint64)
+    s.KRPDrawSamples(N + 1, samples2)
+    ref2 = o.draw(N + 1, O.philox_uniforms(seed, 2 * N * J, 2 * N * J), want_margin=True)
+    check_indices(samples2, ref2, o.margin, list(range(N)))
+
+
+@pytest.mark.parametrize("N,dims,R,J,j", [
+    (4, [1000] * 4, 8, 10000, 5),
+    (3, [4096, 2048, 3000], 32, 4000, 1),
+    (2, [5000, 3000], 64, 2000, 3),
+])
+def test_fp32_draw_agrees_with_fp64_oracle(ftl, N, dims, R, J, j):
+    rng = np.random.default_rng(31 + R)
+    U = [rng.normal(size=(n, R)) for n in dims]
+    draws = rng.random(2 * N * J)
+    s = ftl.Sampler(U, J, R, "efficient", precision="fp32")
+    samples = np.zeros((N, J), dtype=np.uint64)
+    h = np.zeros((J, R))
+    w = np.zeros(J)
+    s.KRPDrawSamples_materialize(j, samples, h, w, draws=draws)
+    o = O.OracleKRPSampler(U, J, R)
+    ref = o.draw(j, draws)
+    rows = included_rows(N, j if j < N else N + 1)
+    agree = (samples[rows] == ref[rows]).all(axis=0)
+    assert agree.mean() >= 0.99, agree.mean()
+    np.testing.assert_allclose(w[agree], o.weights[agree], rtol=1e-3)
+    assert np.array_equal(h[agree], o.h[agree])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_distribution_matches_exact_leverage(ftl, precision):
+    """Empirical distribution of 2^26 draws from the KRP of three 8 x 8
+    factors (512 rows, 1% of entries x10 as in the reference's distribution
+    check) against the brute-force FP64 leverage scores."""
+    rng = np.random.default_rng(2023)
+    N, I, R = 3, 8, 8
+    U = [rng.normal(size=(I, R)) for _ in range(N)]
+    for u in U:
+        u[rng.random(u.shape) < 0.01] *= 10.0
+    lev = O.krp_leverage(U)
+    p = lev / lev.sum()
+    J = 1 << 23
+    s = ftl.Sampler(U, J, R, "efficient", precision=precision, seed=99)
+    counts = torch.zeros(I ** N, dtype=torch.int64, device="cuda")
+    offs = torch.tensor([I ** (N - 1 - k) for k in range(N)], device="cuda", dtype=torch.int64)
+    reps = 8
+    w_err = 0.0
+    for _ in range(reps):
+        samples, h, w = s.draw(N + 1)
+        flat = (samples * offs[:, None]).sum(0)
+        counts += torch.bincount(flat, minlength=I ** N)
+        lev_s = torch.from_numpy(lev).cuda()[flat]
+        w_err = max(w_err, float(((w * J * lev_s / R) - 1).abs().max()))
+    emp = counts.cpu().numpy() / (reps * J)
+    tv = 0.5 * np.abs(emp - p).sum()
+    noise = 0.5 * np.sum(np.sqrt(2 * p / (np.pi * reps * J)))
+    assert tv <= 1.3 * noise + 1e-4, (tv, noise)
+    assert tv < 1e-3
+    assert w_err < (1e-9 if precision == "fp64" else 1e-3), w_err
+
+
+# ---------------------------------------------------------------- tree level
+
+@pytest.mark.parametrize("name", tree_cases())
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_tree_build_and_sample_match_reference_golden(ftl, name, precision):
+    c = load_tree(name)
+    n, F, R, J = (int(c[k]) for k in ("n", "F", "R", "J"))
+    t = ftl.PartitionTree(n, F, J, R, precision=precision)
+    t.build_tree(c["U"])
+    G = t.get_G()
+    scale = np.abs(c["G_packed"]).max()
+    tol = 1e-12 if precision == "fp64" else 2e-6
+    np.testing.assert_allclose(G, c["G_packed"], rtol=0, atol=tol * scale * max(1, np.log2(n)))
+    G0 = np.zeros((R, R))
+    t.get_G0(G0)
+    assert np.array_equal(np.tril(G0, -1), np.zeros((R, R)))
+    h = c["h"].copy()
+    samples = np.zeros(J, dtype=np.uint64)
+    t.PTSample(c["U"], h, c["scaled_h"], samples, c["draws"])
+    if precision == "fp64":
+        Go = O.tree_build(c["U"], F)
+        margin = np.zeros(J)
+        s_o = np.zeros(J, dtype=np.uint64)
+        O.pt_sample(Go, c["U"], F, c["h"].copy(), np.ascontiguousarray(c["scaled_h"]), s_o,
+                    c["draws"], margin)
+        mism = samples != c["samples"]
+        assert np.all(margin[mism] < NEAR_TIE)
+        assert np.array_equal(h[~mism], c["h_out"][~mism])
+    else:
+        assert (samples == c["samples"]).mean() >= 0.99
+
+
+def test_tree_scale_matches_oracle(ftl):
+    rng = np.random.default_rng(5)
+    n, F, R = 500, 8, 8
+    U = rng.normal(size=(n, R))
+    mat = rng.normal(size=(R, R))
+    t = ftl.PartitionTree(n, F, 10, R, precision="fp64")
+    t.build_tree(U)
+    t.multiply_against_numpy_buffer(mat)
+    t.multiply_against_numpy_buffer(mat)  # applied to the unmultiplied Grams again
+    Go = O.tree_scale(O.tree_build(U, F), R, O.upper_to_packed(mat, R))
+    np.testing.assert_allclose(t.get_G(), Go, rtol=1e-13, atol=1e-13)
+
+
+def test_large_tree_build_fp32_vs_fp64(ftl):
+    """Complete tree of 2^20 rows, R = 32: FP32 build within FP32 rounding of
+    the FP64 build at every node."""
+    rng = np.random.default_rng(9)
+    n, R = 1 << 20, 32
+    U = rng.normal(size=(n, R))
+    t64 = ftl.PartitionTree(n, R, 1, R, precision="fp64")
+    t32 = ftl.PartitionTree(n, R, 1, R, precision="fp32")
+    t64.build_tree(U)
+    t32.build_tree(U)
+    a, b = t64.get_G(), t32.get_G()
+    diag = np.array([k * R - k * (k - 1) // 2 for k in range(R)])
+    node_scale = a[:, diag].max(axis=1, keepdims=True)
+    assert np.max(np.abs(a - b) / node_scale) < 1e-5
+    # root against numpy
+    Gr = U.T @ U
+    np.testing.assert_allclose(a[0], Gr[np.triu_indices(R)], rtol=1e-10, atol=1e-8)
