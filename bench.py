@@ -1,0 +1,417 @@
+#!/usr/bin/env python
+"""Headline benchmark: exact Khatri-Rao-product leverage-score sampling.
+
+Workload (the reference's headline sampling configuration): N = 3 factor
+matrices of I = 2^23 rows x R = 32 columns, float64 N(0,1) entries with 1% of
+each factor's rows scaled x100 (seeded, synthetic -- no dataset), J = 50,000
+samples per draw from the full Khatri-Rao product (no mode excluded, the
+reference's KRPDrawSamples(N+1)).  One step = one draw: computeM (Hadamard
+products, FP64 pseudo-inverse and eigendecompositions, eigen trees) plus the
+fused descent of all modes plus the weights, with the partition trees
+resident in HBM.  The trees (3 x 1.1 GB FP32, 3 x 2.2 GB FP64) are larger
+than L2, so no separate flush is done between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|fp64]
+  python bench.py --impl reference ...   # the reference arm: the CPU oracle port
+
+Multi-GPU (torchrun): every rank runs an independent replica of the workload
+(sampling needs no exchange); value = all samples / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "samples/s at I=2^23,R=32 (exact KRP leverage sampling, N=3, J=50000)"
+UNIT = "samples/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--N", type=int, default=3)
+    ap.add_argument("--log2I", type=int, default=23)
+    ap.add_argument("--R", type=int, default=32)
+    ap.add_argument("--J", type=int, default=50000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-arm", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------- distributed
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        exe = shutil.which("nvidia-smi")
+        if not exe:
+            return
+        self.proc = subprocess.Popen(
+            [exe, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+             "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- workload
+
+def make_factors_device(N, I, R, seed, device):
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    U = []
+    for _ in range(N):
+        u = torch.randn(I, R, device=device, dtype=torch.float64, generator=g)
+        rows = torch.randperm(I, device=device, generator=g)[: max(1, I // 100)]
+        u[rows] *= 100.0
+        U.append(u)
+    return U
+
+
+def algorithmic_bytes(samples, dims, R, J, N, j, prec_bytes):
+    """Bytes one descent launch must move at minimum (each distinct node or
+    leaf block read once): per included mode, distinct Gram-tree nodes read
+    (root + left child of every internal node on a sampled path) x P x s_G,
+    distinct leaf blocks x rows x R x 8 (FP64 factor rows of the leaf scan),
+    the whole eigen tree (2R-1) x P x s_G and its R x R FP64 row table; plus
+    the outputs (samples N x J x 8, h J x R x 8, weights J x 8)."""
+    import torch
+    from fast_tensor_leverage_gb300 import _lib
+    P = R * (R + 1) // 2
+    total = 0
+    for k in range(N):
+        if k == j:
+            continue
+        F = min(R, dims[k])
+        g = _lib.tree_geometry(dims[k], F)
+        rows = samples[k].to(torch.int64)
+        leaf = rows // F
+        partial = g.node_count - g.nodes_upto_lfill
+        node = torch.where(leaf < partial, g.nodes_upto_lfill + leaf, leaf + g.complete_level_offset)
+        leaves = torch.unique(leaf)
+        reads = [torch.zeros(1, dtype=torch.int64, device=rows.device)]
+        cur = node
+        while True:
+            cur = cur[cur > 0]
+            if cur.numel() == 0:
+                break
+            parent = (cur - 1) // 2
+            reads.append(torch.unique(2 * parent + 1))
+            cur = torch.unique(parent)
+        n_nodes = int(torch.unique(torch.cat(reads)).numel())
+        total += n_nodes * P * prec_bytes + int(leaves.numel()) * F * R * 8
+        total += (2 * R - 1) * P * prec_bytes + R * R * 8
+    n_inc = sum(1 for k in range(N) if k != j)
+    total += n_inc * J * 8 + J * R * 8 + J * 8
+    return total
+
+
+def read_traffic(precision):
+    """dram bytes per launch of the descent kernel from the committed ncu
+    summary (profiles/krp_draw_kernel_*.md, line 'traffic_bytes_per_launch')."""
+    for f in sorted((REPO / "profiles").glob(f"krp_draw_kernel_{precision}_*.md")):
+        for line in f.read_text().splitlines():
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+def measured_peak():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------ our arm
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import fast_tensor_leverage_gb300 as ftl
+    from fast_tensor_leverage_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    N, I, R, J = args.N, 1 << args.log2I, args.R, args.J
+    j = N + 1
+    U = make_factors_device(N, I, R, 1234 + rank, dev)
+    st = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def time_draws(sampler, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            sampler.draw(j)
+        barrier()
+        torch.cuda.synchronize(dev)
+        if clocks:
+            clocks.start()
+            time.sleep(0.25)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            sampler.draw(j)
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        barrier()
+        clk = clocks.stop() if clocks else None
+        ms = e0.elapsed_time(e1) / steps
+        if ws > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, clk
+
+    s = ftl.Sampler(U, J, R, "efficient", precision=args.precision, seed=7 + rank)
+    clocks = ClockSampler(local) if rank == 0 else None
+    ms, clk = time_draws(s, args.steps, args.warmup, clocks)
+    value = ws * J / (ms / 1e3)
+
+    # descent kernel alone (roofline): computeM once, then timed launches
+    _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), j, st.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ksteps = max(20, args.steps // 3)
+    for _ in range(3):
+        _lib.call("ftl_krp_sample", ctypes.byref(s._plan), j, s.samples_dev.data_ptr(),
+                  s.h_dev.data_ptr(), s.weights_dev.data_ptr(), None, s.seed, 0, st.cuda_stream)
+    e0.record(st)
+    for i in range(ksteps):
+        _lib.call("ftl_krp_sample", ctypes.byref(s._plan), j, s.samples_dev.data_ptr(),
+                  s.h_dev.data_ptr(), s.weights_dev.data_ptr(), None, s.seed,
+                  (i + 1) * 2 * N * J, st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    kernel_ms = e0.elapsed_time(e1) / ksteps
+    prec_bytes = 4 if args.precision == "fp32" else 8
+    alg = algorithmic_bytes(s.samples_dev, s.dims, R, J, N, j, prec_bytes)
+    peak, peak_kind = measured_peak()
+    achieved = alg / (kernel_ms / 1e3) / 1e9
+    traffic = read_traffic(args.precision)
+
+    # end to end through the public numpy API: host uniforms in (pinned),
+    # samples / h / weights back into host arrays, every step
+    e2e_steps = max(5, min(50, args.steps // 5))
+    draws_host = torch.empty(2 * N * J, dtype=torch.float64, pin_memory=True)
+    draws_host.uniform_(0.0, 1.0, generator=torch.Generator().manual_seed(99))
+    samples_np = np.zeros((N, J), dtype=np.uint64)
+    h_np = np.zeros((J, R))
+    w_np = np.zeros(J)
+    for _ in range(3):
+        s.KRPDrawSamples_materialize(j, samples_np, h_np, w_np, draws=draws_host)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.KRPDrawSamples_materialize(j, samples_np, h_np, w_np, draws=draws_host)
+    t_e2e = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": ws * J * e2e_steps / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": 2 * N * J * 8,
+           "d2h_bytes_per_step": N * J * 8 + J * R * 8 + J * 8,
+           "api": "Sampler.KRPDrawSamples_materialize(j, samples, h_out, weights_out, draws=pinned host uniforms)"}
+
+    # the plain FP64 GPU path on the same workload, for the mixed/FP64 ratio
+    fp64 = None
+    if args.precision == "fp32" and not args.no_fp64_arm:
+        del s
+        torch.cuda.empty_cache()
+        s64 = ftl.Sampler(U, J, R, "efficient", precision="fp64", seed=7 + rank)
+        ms64, _ = time_draws(s64, max(10, args.steps // 5), max(3, args.warmup // 4))
+        fp64 = {"value": ws * J / (ms64 / 1e3), "ms_per_step": ms64}
+        del s64
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        U_host = [u.cpu().numpy() for u in U]
+        del U
+        torch.cuda.empty_cache()
+        cpu = cpu_baseline(U_host, J, R, j, reps=3)
+
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.precision, "data": "synthetic (seeded N(0,1), 1% rows x100)",
+        "config": {"workload": "exact KRP leverage sampling, N=3, I=2^23, R=32, J=50000, no mode excluded",
+                   "N": N, "I": I, "R": R, "J": J, "j": j, "precision": args.precision,
+                   "l2": "inputs larger than L2 (partition trees 3 x %.2f GB)" % (
+                       (2 * (I // R) - 1) * (R * (R + 1) // 2) * prec_bytes / 1e9),
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "krp_draw_kernel", "kernel_ms": kernel_ms,
+                     "algorithmic_bytes_per_launch": alg},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    if fp64 is not None:
+        line["fp64_path"] = fp64
+        line["mixed_vs_fp64"] = value / fp64["value"]
+    return line
+
+
+def cpu_baseline(U_host, J, R, j, reps=3):
+    """The CPU oracle port (C restatement of the reference's sampler with
+    OpenMP over samples) on the same workload: full-size trees (built outside
+    the timing), one warm-up draw, median of `reps` draws of J samples."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    N = len(U_host)
+    o = O.OracleKRPSampler(U_host, J, R)
+    rng = np.random.default_rng(5)
+    draws = rng.random(2 * N * J)
+    o.draw(j, draws)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        o.draw(j, draws)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return {"value": J / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} draws of J={J} (median) at the full workload, trees prebuilt"}
+
+
+# ------------------------------------------------------- reference arm
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    N, I, R, J = args.N, 1 << args.log2I, args.R, args.J
+    j = N + 1
+    rng = np.random.default_rng(1234)
+    U = []
+    for _ in range(N):
+        u = rng.standard_normal((I, R))
+        u[rng.choice(I, size=max(1, I // 100), replace=False)] *= 100.0
+        U.append(u)
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    # each step: one draw of J_step samples (bounded so the run stays short)
+    J_step = min(J, 10000)
+    o = O.OracleKRPSampler(U, J_step, R)
+    draws = rng.random(2 * N * J_step)
+    for _ in range(max(1, args.warmup)):
+        o.draw(j, draws)
+    steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.draw(j, draws)
+    t = time.perf_counter() - t0
+    value = steps * J_step / t
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded N(0,1), 1% rows x100)",
+        "config": {"workload": "exact KRP leverage sampling, N=3, I=2^23, R=32, J=50000, no mode excluded",
+                   "N": N, "I": I, "R": R, "J": J, "j": j, "samples_per_step": J_step},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} draws of {J_step} samples at the full workload"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        line = run_reference(args, ws, rank)
+    else:
+        line = run_ours(args, ws, rank, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if ws > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -170,15 +170,55 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int P, c
 
 // ------------------------------------------------------------- leaf scan
 
+// The warp's staged query as per-lane registers (entry lane + 32q in [q]).
+template <int RMAX, typename T>
+struct LaneQuery {
+    T v[Shape<RMAX>::XPL];
+};
+
+template <int RMAX, typename T>
+__device__ __forceinline__ LaneQuery<RMAX, T> lane_query(const T *x, int R, int lane) {
+    LaneQuery<RMAX, T> q;
+#pragma unroll
+    for (int i = 0; i < Shape<RMAX>::XPL; ++i) {
+        int col = lane + 32 * i;
+        q.v[i] = col < R ? x[col] : T(0);
+    }
+    return q;
+}
+
+// Sum over lanes of 32 per-lane values at once: afterwards lane l holds
+// sum_lanes v[l] in v[0] (butterfly that halves the live values per stage,
+// 31 shuffles instead of 32 x 5).
+template <typename T>
+__device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < off; ++i) {
+            T send = upper ? v[i] : v[i + off];
+            T keep = upper ? v[i + off] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    return v[0];
+}
+
 // Row selection inside leaf block c (F > 1): q_r = U[row0+r] . x for the
 // block's rows, inclusive prefix of q_r^2 in row order, first r <= F-2 with
-// frac < prefix_r / total, else F-1.  x is the warp's query in the compute
-// type (shared memory).  A selection past the last row of a partial block
-// (only reachable when frac rounds to >= 1) is clamped to that last row.
+// frac < prefix_r / total, else F-1.  The block is read row by row with
+// coalesced loads (lane = column), all issued before any use, and the 32 row
+// dot products are finished by one transpose-reduce.  xq holds the warp's
+// query in the compute type.  A selection past
+// the last row of a partial block (only reachable when frac rounds to >= 1)
+// is clamped to that last row.
 template <int RMAX, typename T>
 __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R, const DGeom &g,
-                                             int64_t c, T frac, const T *x, int lane) {
+                                             int64_t c, T frac, const LaneQuery<RMAX, T> &xq,
+                                             int lane) {
     constexpr int FQ = Shape<RMAX>::FQ;
+    constexpr int XPL = Shape<RMAX>::XPL;
     const int64_t leaf = leaf_index(g, c);
     const int F = (int)g.F;
     const int64_t row0 = leaf * g.F;
@@ -186,12 +226,22 @@ __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R
     T q2[FQ];
 #pragma unroll
     for (int qi = 0; qi < FQ; ++qi) {
-        int r = lane + 32 * qi;
-        T q = T(0);
-        if (r < rows) {
-            const double *u = U + (row0 + r) * (int64_t)R;
-            for (int col = 0; col < R; ++col) q = fma((T)__ldg(u + col), x[col], q);
+        T v[32];
+#pragma unroll
+        for (int rr = 0; rr < 32; ++rr) {
+            const int r = 32 * qi + rr;
+            T acc = T(0);
+            if (r < rows) {
+                const double *u = U + (row0 + r) * (int64_t)R;
+#pragma unroll
+                for (int q = 0; q < XPL; ++q) {
+                    const int col = lane + 32 * q;
+                    if (col < R) acc = fma((T)__ldg(u + col), xq.v[q], acc);
+                }
+            }
+            v[rr] = acc;
         }
+        T q = transpose_reduce32<T>(v, lane);
         q2[qi] = q * q;
     }
     T incl[FQ];

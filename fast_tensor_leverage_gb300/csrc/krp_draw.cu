@@ -42,7 +42,7 @@ __device__ __forceinline__ double get_draw(const DrawParams &p, int64_t idx) {
 }
 
 template <int RMAX, typename T>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_draw_kernel(DrawParams p) {
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 1024 : 512) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_draw_kernel(DrawP
             const DGeom &g = p.gram[k];
             c = descend<RMAX>((const T *)p.gram_G[k], P, g,
                               get_draw(p, (int64_t)(p.N + k) * p.J + i), qf, lane, frac);
-            int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(p.U[k], R, g, c, frac, xT, lane)
+            int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(p.U[k], R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
                                 : leaf_index(g, c);
             const double *Ur = p.U[k] + t * R;
 #pragma unroll
@@ -137,7 +137,7 @@ struct TreeSampleParams {
 // PartitionTree::PTSample_internal (cpp_ext/partition_tree.hpp:232-405):
 // x = scaled_h[i]; samples[i] = selected row; h[i] o= U[row].
 template <int RMAX, typename T>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) tree_sample_kernel(TreeSampleParams p) {
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 1024 : 512) / (Shape<RMAX>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) tree_sample_kernel(Tr
         qf.setup(xT, pairs, lane);
         T frac;
         int64_t c = descend<RMAX>((const T *)p.G, P, p.g, p.draws[i], qf, lane, frac);
-        int64_t t = p.g.F > 1 ? leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, xT, lane)
+        int64_t t = p.g.F > 1 ? leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
                               : leaf_index(p.g, c);
         if (lane == 0) p.samples[i] = (uint64_t)t;
 #pragma unroll
@@ -286,12 +286,12 @@ extern "C" int ftl_krp_compute_m(const ftl_krp_plan *plan, uint32_t j, void *str
     return computem_launch(plan, jn, (cudaStream_t)stream);
 }
 
-extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
-                            double *weights, const double *draws, uint64_t seed, uint64_t ctr,
-                            void *stream) {
-    int rc = ftl_krp_compute_m(plan, j, stream);
+extern "C" int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
+                              double *weights, const double *draws, uint64_t seed, uint64_t ctr,
+                              void *stream) {
+    int rc = validate_plan(plan);
     if (rc) return rc;
-    FTL_CHECK_ARG(samples != nullptr, "ftl_krp_draw: samples is NULL");
+    FTL_CHECK_ARG(samples != nullptr, "ftl_krp_sample: samples is NULL");
     DrawParams p;
     p.N = plan->N;
     p.R = plan->R;
@@ -324,6 +324,14 @@ extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samp
     cudaStream_t st = (cudaStream_t)stream;
     if (plan->prec == FTL_PREC_FP64) return dispatch_draw<double>(p, st);
     return dispatch_draw<float>(p, st);
+}
+
+extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
+                            double *weights, const double *draws, uint64_t seed, uint64_t ctr,
+                            void *stream) {
+    int rc = ftl_krp_compute_m(plan, j, stream);
+    if (rc) return rc;
+    return ftl_krp_sample(plan, j, samples, h, weights, draws, seed, ctr, stream);
 }
 
 extern "C" int ftl_tree_sample(const void *G, int prec, const double *U, int64_t n, int R, int64_t F,

@@ -37,7 +37,7 @@ class Sampler:
             raise ValueError(f"R={R} outside [1, {_lib.MAX_RANK}]")
         if J < 1:
             raise ValueError(f"J={J} must be positive")
-        factors = [D.as_factor(u, R, f"matrices[{k}]") for k, u in enumerate(U)]
+        factors = [self._factor_input(u, R, f"matrices[{k}]") for k, u in enumerate(U)]
         self.N, self.J, self.R = N, J, R
         self.precision = precision
         self._prec = _lib.PREC[precision]
@@ -47,7 +47,8 @@ class Sampler:
         self.P = R * (R + 1) // 2
         tdt = torch.float64 if precision == "fp64" else torch.float32
         dev = self.device
-        self.U = [torch.from_numpy(f).to(dev) for f in factors]
+        self.U = [f.to(dev, torch.float64).contiguous() if isinstance(f, torch.Tensor)
+                  else torch.from_numpy(f).to(dev) for f in factors]
         self.trees = []
         for k in range(N):
             nb = _lib.tree_bytes(self.dims[k], self.F[k], R, self._prec)
@@ -67,6 +68,15 @@ class Sampler:
         self._refresh_plan()
         for k in range(N):
             self.update_sampler(k)
+
+    @staticmethod
+    def _factor_input(u, R: int, name: str):
+        # CUDA tensors stay on the device; everything else becomes float64 numpy
+        if isinstance(u, torch.Tensor) and u.is_cuda:
+            if u.dim() != 2 or u.shape[1] != R or u.shape[0] < 1:
+                raise ValueError(f"{name} must be (I, {R}), got {tuple(u.shape)}")
+            return u
+        return D.as_factor(u, R, name)
 
     # ----------------------------------------------------------- plumbing
     def _refresh_plan(self) -> None:

@@ -147,6 +147,14 @@ int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples_dev,
                  double *h_dev, double *weights_dev, const double *draws_dev,
                  uint64_t seed, uint64_t ctr, void *stream);
 
+/* The descent part of ftl_krp_draw alone: uses the computeM state left in
+ * the plan's workspaces by the last ftl_krp_compute_m for the same j (and
+ * unchanged trees).  Lets callers amortise computeM over several batches of
+ * J samples. */
+int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples_dev,
+                   double *h_dev, double *weights_dev, const double *draws_dev,
+                   uint64_t seed, uint64_t ctr, void *stream);
+
 /* Fill out_dev[0..n) with the uniforms the in-kernel generator uses
  * (Philox4x32-10, key=seed, counter=ctr+i). */
 int ftl_philox_uniforms(double *out_dev, int64_t n, uint64_t seed, uint64_t ctr,

@@ -103,16 +103,21 @@ void orc_tree_scale(const double *src, double *dst, int64_t node_count, int R, c
 }
 
 /* x^T G x as the reference evaluates it: y = G x with G symmetric from its
- * upper triangle (cblas_dsymv, partition_tree.hpp:66-81), then the
- * sequential dot product of batch_dot_product (:201-214). */
+ * upper triangle (cblas_dsymv, partition_tree.hpp:66-81; here the textbook
+ * upper-triangle dsymv loop over the packed rows), then the sequential dot
+ * product of batch_dot_product (:201-214). */
 static double qform(const double *Gn, const double *x, int R, double *y) {
+    for (int a = 0; a < R; a++) y[a] = 0.0;
+    const double *row = Gn;
     for (int a = 0; a < R; a++) {
-        double acc = 0.0;
-        for (int b = 0; b < R; b++) {
-            int lo = a < b ? a : b, hi = a < b ? b : a;
-            acc += Gn[pk(lo, hi, R)] * x[b];
+        const double xa = x[a];
+        double acc = row[0] * xa;
+        for (int b = a + 1; b < R; b++) {
+            acc += row[b - a] * x[b];
+            y[b] += row[b - a] * xa;
         }
-        y[a] = acc;
+        y[a] += acc;
+        row += R - a;
     }
     double m = 0.0;
     for (int a = 0; a < R; a++) m += x[a] * y[a];

@@ -31,7 +31,7 @@ def build(force: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     tmp = BUILD / "libftl_oracle.so.tmp"
-    cmd = ["gcc", "-O2", "-fopenmp", "-shared", "-fPIC", "-std=c11", str(src), "-o", str(tmp), "-lm"]
+    cmd = ["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-std=c11", str(src), "-o", str(tmp), "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
     return LIB
