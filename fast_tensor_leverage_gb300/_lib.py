@@ -78,6 +78,7 @@ SIGNATURES = {
     "ftl_krp_compute_m": ([ctypes.POINTER(KRPPlan), _U32, _P], _INT),
     "ftl_krp_draw": ([ctypes.POINTER(KRPPlan), _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
     "ftl_krp_sample": ([ctypes.POINTER(KRPPlan), _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
+    "ftl_krp_draw_static": ([_INT, _INT, _I64, _INT, _P, _P, _P, _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
     "ftl_philox_uniforms": ([_P, _I64, _U64, _U64, _P], _INT),
 }
 

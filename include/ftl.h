@@ -115,7 +115,7 @@ typedef struct ftl_krp_plan {
     const double *U[FTL_MAX_MODES];      /* device factors, dims[k] x R */
     void *gram_G[FTL_MAX_MODES];         /* device Gram trees, F = min(R, dims[k]) */
     void *eig_G;                         /* device, N x (2R-1) x P, prec */
-    double *M;                           /* device workspace, (N+2) x R x R FP64 */
+    double *M;                           /* device workspace, (2N+3) x R x R FP64 */
     double *lambda;                      /* device workspace, (N+1) x R FP64 */
     float *pinv32;                       /* device workspace, P FP32 (FP32 weights) */
 } ftl_krp_plan;
@@ -154,6 +154,29 @@ int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples_dev,
 int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples_dev,
                    double *h_dev, double *weights_dev, const double *draws_dev,
                    uint64_t seed, uint64_t ctr, void *stream);
+
+/* Size of the device array that ftl_krp_draw_static uses for scratch. */
+#define FTL_DRAW_STATIC_SCRATCH_BYTES (8u << 20)
+
+/* ftl_krp_draw for callers that cannot allocate device memory.  No
+ * counterpart in the reference (its sampler allocates host buffers freely).
+ * Some callers cannot call cudaMalloc: hosts that reserve their whole device
+ * budget up front through another runtime (cgo/JNI/FFI integrations), or a
+ * request path that must not allocate because cudaMalloc can synchronise the
+ * device or fail under memory pressure.  Same inputs and outputs as
+ * ftl_krp_draw, without workspaces: the eigen trees, computeM matrices,
+ * eigenvalues and FP32 pseudo-inverse live in one static device array of
+ * FTL_DRAW_STATIC_SCRATCH_BYTES that every GPU loading the library holds
+ * until exit.  Configurations needing more (N x (2R-1) x P tree values plus
+ * (2N+3) x R x R FP64, e.g. beyond N=16 at R=32) return FTL_E_ARG.  The
+ * first call on a device looks up the array's address with that device
+ * current; make it before any stream capture.  All calls share the array
+ * (each clears the part it uses): calls that overlap on the GPU race and
+ * must be serialised by the caller.  Allocates nothing. */
+int ftl_krp_draw_static(int N, int R, int64_t J, int prec, const int64_t *dims,
+                        const double *const *U_dev, void *const *gram_G_dev, uint32_t j,
+                        uint64_t *samples_dev, double *h_dev, double *weights_dev,
+                        const double *draws_dev, uint64_t seed, uint64_t ctr, void *stream);
 
 /* Fill out_dev[0..n) with the uniforms the in-kernel generator uses
  * (Philox4x32-10, key=seed, counter=ctr+i). */
