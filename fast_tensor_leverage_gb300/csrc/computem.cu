@@ -219,6 +219,9 @@ __global__ void computem_pinv_kernel(CMParams p) {
             p.pinv32[pe] = (float)A[e];
         }
     }
+    // zero padding up to the node strides, read by the vectorised forms
+    for (int e = p.P + tid; e < node_stride(R, 8); e += nth) pinv_packed[e] = 0.0;
+    for (int e = p.P + tid; e < node_stride(R, 4); e += nth) p.pinv32[e] = 0.0f;
     // M[k] o= pinv for k = N-1 .. 1, k != j
     for (int k = N - 1; k >= 1; --k) {
         if ((uint32_t)k == p.j) continue;
@@ -256,36 +259,41 @@ __global__ void computem_eig_kernel(CMParams p) {
         __syncthreads();
     }
     // Eigen tree over the R rows of W (F = 1): leaves, child sums, then o root.
-    T *G = (T *)p.eig_G + (size_t)k * (2 * R - 1) * P;
+    const int S = node_stride(R, sizeof(T));
+    T *G = (T *)p.eig_G + (size_t)k * (2 * R - 1) * S;
     const DGeom g = p.eig;
     const int leaf_count = R;
-    for (int e = tid; e < leaf_count * P; e += nth) {
-        int u = e / P, pe = e - u * P;
-        int a = 0, rem = pe;
-        while (rem >= R - a) {
-            rem -= R - a;
-            ++a;
+    for (int e = tid; e < leaf_count * S; e += nth) {
+        int u = e / S, pe = e - u * S;
+        T v = T(0);
+        if (pe < P) {
+            int a = 0, rem = pe;
+            while (rem >= R - a) {
+                rem -= R - a;
+                ++a;
+            }
+            int b = a + rem;
+            v = (T)W[u * R + a] * (T)W[u * R + b];
         }
-        int b = a + rem;
-        G[leaf_node(g, u) * P + pe] = (T)W[u * R + a] * (T)W[u * R + b];
+        G[leaf_node(g, u) * S + pe] = v;
     }
     __syncthreads();
     int64_t start = g.nodes_upto_lfill - ((g.nodes_upto_lfill + 1) / 2);  // nodes_before_lfill
     int64_t end = g.node_count - leaf_count;
     while (true) {
-        for (int64_t e = tid; e < (end - start) * P; e += nth) {
-            int64_t c = start + e / P;
-            int pe = (int)(e % P);
-            G[c * P + pe] = G[(2 * c + 1) * P + pe] + G[(2 * c + 2) * P + pe];
+        for (int64_t e = tid; e < (end - start) * S; e += nth) {
+            int64_t c = start + e / S;
+            int pe = (int)(e % S);
+            G[c * S + pe] = G[(2 * c + 1) * S + pe] + G[(2 * c + 2) * S + pe];
         }
         __syncthreads();
         if (start <= 0) break;
         end = start;
         start = (start + 1) / 2 - 1;
     }
-    for (int64_t e = tid; e < (int64_t)(2 * R - 1) * P; e += nth) {
-        int pe = (int)(e % P);
-        G[e] = G[e] * (T)root_at(p, k, pe);
+    for (int64_t e = tid; e < (int64_t)(2 * R - 1) * S; e += nth) {
+        int pe = (int)(e % S);
+        if (pe < P) G[e] = G[e] * (T)root_at(p, k, pe);
     }
 }
 

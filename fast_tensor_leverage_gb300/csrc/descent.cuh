@@ -27,43 +27,71 @@ namespace ftl {
 template <int RMAX>
 struct Shape {
     static constexpr int PMAX = RMAX * (RMAX + 1) / 2;
-    static constexpr int VPL = (PMAX + 31) / 32;  // packed values per lane
     static constexpr int XPL = (RMAX + 31) / 32;  // vector entries per lane
     static constexpr int FQ = (RMAX + 31) / 32;   // leaf rows per lane (F <= R)
     static constexpr bool XX_SMEM = RMAX > 32;
     static constexpr int WARPS = RMAX <= 32 ? 8 : (RMAX <= 64 ? 4 : 2);
 };
 
+// 16-byte vector of the tree precision.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    static constexpr int W = 4;
+    static __device__ __forceinline__ void get(const type &v, float (&o)[4]) {
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+        o[3] = v.w;
+    }
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+    static constexpr int W = 2;
+    static __device__ __forceinline__ void get(const type &v, double (&o)[2]) {
+        o[0] = v.x;
+        o[1] = v.y;
+    }
+};
+
+// Node geometry of one precision: S = node stride (packed triangle padded to
+// 16 bytes), NV = 16-byte vectors per lane to cover the largest node.
+template <int RMAX, typename T>
+struct NodeShape {
+    static constexpr int W = Vec16<T>::W;
+    static constexpr int SMAX = (Shape<RMAX>::PMAX + W - 1) / W * W;
+    static constexpr int NV = (SMAX / W + 31) / 32;
+};
+
 // Per-warp shared-memory slot: the query in FP64 and in the compute type,
 // plus the packed outer product when it does not fit in registers.
 template <int RMAX, typename T>
 struct WarpSlot {
-    static constexpr size_t xx_elems = Shape<RMAX>::XX_SMEM ? Shape<RMAX>::PMAX : 0;
+    static constexpr size_t xx_elems = Shape<RMAX>::XX_SMEM ? NodeShape<RMAX, T>::SMAX : 0;
     static constexpr size_t bytes =
         ((RMAX * sizeof(double) + RMAX * sizeof(T) + xx_elems * sizeof(T)) + 15) / 16 * 16;
 };
 
+// x^T G x for one query x against any node G (packed, node stride S): the
+// node is read as 16-byte vectors, vector v of lane l is v = l + 32 t, and
+// the matching weighted outer-product values live in registers (R <= 32) or
+// in the warp's shared-memory slot.
 template <int RMAX, typename T>
 struct QForm {
-    using S = Shape<RMAX>;
-    T r[S::XX_SMEM ? 1 : S::VPL];
+    using S_ = Shape<RMAX>;
+    using NS = NodeShape<RMAX, T>;
+    using V = typename Vec16<T>::type;
+    static constexpr int W = NS::W;
+    T r[S_::XX_SMEM ? 1 : NS::NV * W];
     T *s;
-    int P;
+    int P, S;
 
     __device__ __forceinline__ void setup(const T *x, const uint16_t *pairs, int lane) {
-        if (S::XX_SMEM) {
-            for (int e = lane; e < P; e += 32) {
-                unsigned pr = pairs[e];
-                int a = pr >> 8, b = pr & 0xff;
-                T v = x[a] * x[b];
-                if (a != b) v += v;
-                s[e] = v;
-            }
-            __syncwarp();
-        } else {
-#pragma unroll
-            for (int t = 0; t < S::VPL; ++t) {
-                int e = lane + 32 * t;
+        if (S_::XX_SMEM) {
+            for (int e = lane; e < S; e += 32) {
                 T v = T(0);
                 if (e < P) {
                     unsigned pr = pairs[e];
@@ -71,38 +99,99 @@ struct QForm {
                     v = x[a] * x[b];
                     if (a != b) v += v;
                 }
-                r[t] = v;
+                s[e] = v;
+            }
+            __syncwarp();
+        } else {
+#pragma unroll
+            for (int t = 0; t < NS::NV; ++t) {
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    int e = (lane + 32 * t) * W + w;
+                    T v = T(0);
+                    if (e < P) {
+                        unsigned pr = pairs[e];
+                        int a = pr >> 8, b = pr & 0xff;
+                        v = x[a] * x[b];
+                        if (a != b) v += v;
+                    }
+                    r[t * W + w] = v;
+                }
             }
         }
     }
 
     __device__ __forceinline__ T eval(const T *__restrict__ node, int lane) const {
         T acc = T(0);
-        if (S::XX_SMEM) {
-#pragma unroll 4
-            for (int e = lane; e < P; e += 32) acc = fma(__ldg(node + e), s[e], acc);
+        if (S_::XX_SMEM) {
+#pragma unroll 2
+            for (int e = lane * W; e < S; e += 32 * W) {
+                V g = __ldg(reinterpret_cast<const V *>(node + e));
+                V x = *reinterpret_cast<const V *>(s + e);
+                T gv[W], xv[W];
+                Vec16<T>::get(g, gv);
+                Vec16<T>::get(x, xv);
+#pragma unroll
+                for (int w = 0; w < W; ++w) acc = fma(gv[w], xv[w], acc);
+            }
         } else {
 #pragma unroll
-            for (int t = 0; t < S::VPL; ++t) {
-                int e = lane + 32 * t;
-                if (e < P) acc = fma(__ldg(node + e), r[t], acc);
+            for (int t = 0; t < NS::NV; ++t) {
+                int e = (lane + 32 * t) * W;
+                if (e < S) {
+                    V g = __ldg(reinterpret_cast<const V *>(node + e));
+                    T gv[W];
+                    Vec16<T>::get(g, gv);
+#pragma unroll
+                    for (int w = 0; w < W; ++w) acc = fma(gv[w], r[t * W + w], acc);
+                }
             }
         }
         return warp_sum(acc);
     }
 };
 
+// L2 prefetch of `bytes` bytes at p, spread over the warp's lanes.
+__device__ __forceinline__ void prefetch_l2(const void *p, int bytes, int lane) {
+    const char *c = (const char *)p;
+    for (int off = lane * 128; off < bytes; off += 32 * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(c + off));
+    if (lane == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + bytes - 1));
+}
+
+// Before evaluating level `c` -> child 2c+1, fetch into L2 what the next step
+// can need: for each child c' of c, its left child's node (next level), or,
+// when c' is a leaf of a tree with a leaf scan, its factor block.
+template <typename T>
+__device__ __forceinline__ void prefetch_next(const T *G, int S, const DGeom &g, int64_t c,
+                                              const double *U, int R, int lane) {
+#pragma unroll
+    for (int side = 1; side <= 2; ++side) {
+        const int64_t cc = 2 * c + side;
+        if (cc >= g.node_count) continue;
+        if (!is_leaf(g, cc)) {
+            prefetch_l2(G + (2 * cc + 1) * (int64_t)S, S * (int)sizeof(T), lane);
+        } else if (U != nullptr) {
+            const int64_t row0 = leaf_index(g, cc) * g.F;
+            const int64_t rows = min(g.F, g.n - row0);
+            prefetch_l2(U + row0 * R, (int)(rows * R * (int64_t)sizeof(double)), lane);
+        }
+    }
+}
+
 // ----------------------------------------------------------------- FP64
 
 template <int RMAX>
-__device__ __forceinline__ int64_t descend(const double *__restrict__ G, int P, const DGeom &g,
+__device__ __forceinline__ int64_t descend(const double *__restrict__ G, int S, const DGeom &g,
                                            double draw, const QForm<RMAX, double> &qf, int lane,
-                                           double &frac) {
+                                           double &frac, const double *U = nullptr, int R = 0) {
     int64_t c = 0;
     double low = 0.0, high = 1.0;
+    if (!is_leaf(g, 0)) prefetch_l2(G + S, S * 8, lane);
     const double m = qf.eval(G, lane);
     for (int64_t lvl = 0; lvl < g.lfill_level; ++lvl) {
-        double mL = qf.eval(G + (2 * c + 1) * (int64_t)P, lane);
+        prefetch_next(G, S, g, c, U, R, lane);
+        double mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
         double cutoff = low + mL / m;
         if (draw <= cutoff) {
             c = 2 * c + 1;
@@ -113,7 +202,8 @@ __device__ __forceinline__ int64_t descend(const double *__restrict__ G, int P, 
         }
     }
     if (!is_leaf(g, c)) {
-        double mL = qf.eval(G + (2 * c + 1) * (int64_t)P, lane);
+        prefetch_next(G, S, g, c, U, R, lane);
+        double mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
         double cutoff = low + mL / m;
         if (draw <= cutoff) {
             c = 2 * c + 1;
@@ -141,10 +231,11 @@ __device__ __forceinline__ void df_sub(float &th, float &tl, float m) {
 }
 
 template <int RMAX>
-__device__ __forceinline__ int64_t descend(const float *__restrict__ G, int P, const DGeom &g,
+__device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, const DGeom &g,
                                            double draw, const QForm<RMAX, float> &qf, int lane,
-                                           float &frac) {
+                                           float &frac, const double *U = nullptr, int R = 0) {
     int64_t c = 0;
+    if (!is_leaf(g, 0)) prefetch_l2(G + S, S * 4, lane);
     float mP = qf.eval(G, lane);
     double t0 = draw * (double)mP;
     float th = (float)t0;
@@ -152,7 +243,8 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int P, c
     int64_t steps = g.lfill_level + 1;
     for (int64_t lvl = 0; lvl < steps; ++lvl) {
         if (lvl == g.lfill_level && is_leaf(g, c)) break;
-        float mL = qf.eval(G + (2 * c + 1) * (int64_t)P, lane);
+        prefetch_next(G, S, g, c, U, R, lane);
+        float mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
         bool left = ((th - mL) + tl) <= 0.0f;
         if (left) {
             c = 2 * c + 1;

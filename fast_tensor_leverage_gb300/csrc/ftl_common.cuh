@@ -85,6 +85,13 @@ __host__ __device__ inline int64_t leaf_node(const DGeom &g, int64_t leaf) {
 // ------------------------------------------------------ packed triangles
 
 __host__ __device__ inline int packed_size(int R) { return R * (R + 1) / 2; }
+// Node stride in elements: the packed triangle padded (with zeros) to a
+// multiple of 16 bytes, so every node starts 16-byte aligned and is read
+// with 128-bit loads.
+__host__ __device__ inline int node_stride(int R, int elem_bytes) {
+    const int w = 16 / elem_bytes;
+    return (packed_size(R) + w - 1) / w * w;
+}
 __host__ __device__ inline int packed_row_offset(int a, int R) { return a * R - a * (a - 1) / 2; }
 __host__ __device__ inline int packed_index(int a, int b, int R) {
     return packed_row_offset(a, R) + (b - a);

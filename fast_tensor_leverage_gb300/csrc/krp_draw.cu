@@ -19,7 +19,7 @@ int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st);
 int num_sms();
 
 struct DrawParams {
-    int N, R, P;
+    int N, R, P, S;
     uint32_t j;
     int64_t J;
     DGeom gram[FTL_MAX_MODES];
@@ -51,15 +51,16 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
     build_pairs(pairs, R);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *slot =
-        smem_raw + ((S::PMAX * sizeof(uint16_t) + 15) / 16 * 16) + warp * WarpSlot<RMAX, T>::bytes;
+    unsigned char *slot = smem_raw + ((NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16) +
+                          warp * WarpSlot<RMAX, T>::bytes;
     double *xd = (double *)slot;
     T *xT = sizeof(T) == 8 ? (T *)xd : (T *)(xd + RMAX);
     QForm<RMAX, T> qf;
     qf.P = P;
+    qf.S = p.S;
     qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
     const size_t RR = (size_t)R * R;
-    const size_t eig_stride = (size_t)(2 * R - 1) * P;
+    const size_t eig_stride = (size_t)(2 * R - 1) * p.S;
 
     for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
          i += (int64_t)gridDim.x * S::WARPS) {
@@ -72,7 +73,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
             stage_query<RMAX, T>(h, R, xd, xT, lane);
             qf.setup(xT, pairs, lane);
             T frac;
-            int64_t c = descend<RMAX>((const T *)p.eig_G + k * eig_stride, P, p.eig,
+            int64_t c = descend<RMAX>((const T *)p.eig_G + k * eig_stride, p.S, p.eig,
                                       get_draw(p, (int64_t)k * p.J + i), qf, lane, frac);
             int64_t u = leaf_index(p.eig, c);
             const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)u * R;
@@ -87,8 +88,9 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
             stage_query<RMAX, T>(xs, R, xd, xT, lane);
             qf.setup(xT, pairs, lane);
             const DGeom &g = p.gram[k];
-            c = descend<RMAX>((const T *)p.gram_G[k], P, g,
-                              get_draw(p, (int64_t)(p.N + k) * p.J + i), qf, lane, frac);
+            c = descend<RMAX>((const T *)p.gram_G[k], p.S, g,
+                              get_draw(p, (int64_t)(p.N + k) * p.J + i), qf, lane, frac,
+                              g.F > 1 ? p.U[k] : nullptr, R);
             int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(p.U[k], R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
                                 : leaf_index(g, c);
             const double *Ur = p.U[k] + t * R;
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
 struct TreeSampleParams {
     const void *G;
     const double *U;
-    int R, P;
+    int R, P, S;
     DGeom g;
     double *h;
     const double *scaled_h;
@@ -146,12 +148,13 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
     build_pairs(pairs, R);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *slot =
-        smem_raw + ((S::PMAX * sizeof(uint16_t) + 15) / 16 * 16) + warp * WarpSlot<RMAX, T>::bytes;
+    unsigned char *slot = smem_raw + ((NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16) +
+                          warp * WarpSlot<RMAX, T>::bytes;
     double *xd = (double *)slot;
     T *xT = sizeof(T) == 8 ? (T *)xd : (T *)(xd + RMAX);
     QForm<RMAX, T> qf;
     qf.P = P;
+    qf.S = p.S;
     qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
     for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
          i += (int64_t)gridDim.x * S::WARPS) {
@@ -164,7 +167,8 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
         stage_query<RMAX, T>(x, R, xd, xT, lane);
         qf.setup(xT, pairs, lane);
         T frac;
-        int64_t c = descend<RMAX>((const T *)p.G, P, p.g, p.draws[i], qf, lane, frac);
+        int64_t c = descend<RMAX>((const T *)p.G, p.S, p.g, p.draws[i], qf, lane, frac,
+                                  p.g.F > 1 ? p.U : nullptr, R);
         int64_t t = p.g.F > 1 ? leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
                               : leaf_index(p.g, c);
         if (lane == 0) p.samples[i] = (uint64_t)t;
@@ -185,7 +189,7 @@ __global__ void philox_fill_kernel(double *out, int64_t n, uint64_t seed, uint64
 
 template <int RMAX, typename T>
 static size_t desc_smem() {
-    return (Shape<RMAX>::PMAX * sizeof(uint16_t) + 15) / 16 * 16 +
+    return (NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16 +
            (size_t)Shape<RMAX>::WARPS * WarpSlot<RMAX, T>::bytes;
 }
 
@@ -268,11 +272,13 @@ extern "C" int ftl_krp_plan_sizes(int N, int R, int prec, size_t *eig_bytes, siz
     FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && R >= 1 && R <= FTL_MAX_RANK,
                   "ftl_krp_plan_sizes: bad N=%d R=%d", N, R);
     FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_krp_plan_sizes: bad precision");
-    const size_t P = (size_t)packed_size(R);
-    if (eig_bytes) *eig_bytes = (size_t)N * (2 * R - 1) * P * (prec == FTL_PREC_FP64 ? 8 : 4);
-    if (M_bytes) *M_bytes = (size_t)(2 * N + 3) * R * R * sizeof(double);
+    const int esize = prec == FTL_PREC_FP64 ? 8 : 4;
+    if (eig_bytes) *eig_bytes = (size_t)N * (2 * R - 1) * node_stride(R, esize) * esize;
+    // slot N+1 holds the packed FP64 pseudo-inverse padded to its node stride,
+    // which can exceed R*R for R = 1: 16 spare doubles at the end
+    if (M_bytes) *M_bytes = ((size_t)(2 * N + 3) * R * R + 16) * sizeof(double);
     if (lambda_bytes) *lambda_bytes = (size_t)(N + 1) * R * sizeof(double);
-    if (pinv32_bytes) *pinv32_bytes = P * sizeof(float);
+    if (pinv32_bytes) *pinv32_bytes = (size_t)node_stride(R, 4) * sizeof(float);
     return FTL_OK;
 }
 
@@ -296,6 +302,7 @@ extern "C" int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *sa
     p.N = plan->N;
     p.R = plan->R;
     p.P = packed_size(plan->R);
+    p.S = node_stride(plan->R, plan->prec == FTL_PREC_FP64 ? 8 : 4);
     p.j = normalise_j(plan, j);
     p.J = plan->J;
     for (int k = 0; k < FTL_MAX_MODES; ++k) {
@@ -347,6 +354,7 @@ extern "C" int ftl_tree_sample(const void *G, int prec, const double *U, int64_t
     p.U = U;
     p.R = R;
     p.P = packed_size(R);
+    p.S = node_stride(R, prec == FTL_PREC_FP64 ? 8 : 4);
     p.g = to_dgeom(make_geom(n, F));
     p.h = h;
     p.scaled_h = scaled_h;

@@ -38,6 +38,7 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
     T *Us = reinterpret_cast<T *>(smem_raw);  // LB x F x RP
     const int64_t F = g.F;
     const int P = packed_size(R);
+    const int S = node_stride(R, sizeof(T));
     const int nt = RP / 4;
     const int tiles = nt * (nt + 1) / 2;
     const int64_t leaf_count = (n + F - 1) / F;
@@ -90,7 +91,9 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
 #pragma unroll
                     for (int y = 0; y < 4; ++y) acc[x][y] = fma(a4[x], b4[y], acc[x][y]);
             }
-            T *Gn = G + leaf_node(g, leaf) * (int64_t)P;
+            T *Gn = G + leaf_node(g, leaf) * (int64_t)S;
+            if (tile == 0)
+                for (int e = P; e < S; ++e) Gn[e] = T(0);
 #pragma unroll
             for (int x = 0; x < 4; ++x) {
                 int a = 4 * ta + x;
@@ -107,24 +110,26 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
     }
 }
 
-// G[c] = G[2c+1] + G[2c+2] for c in [start, end).
+// G[c] = G[2c+1] + G[2c+2] for c in [start, end) (S = node stride; the
+// zero padding sums to zero).
 template <typename T>
-__global__ void level_sum_kernel(T *__restrict__ G, int64_t start, int64_t end, int P) {
-    const int64_t total = (end - start) * (int64_t)P;
+__global__ void level_sum_kernel(T *__restrict__ G, int64_t start, int64_t end, int S) {
+    const int64_t total = (end - start) * (int64_t)S;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = start + e / P;
-        int k = (int)(e % P);
-        G[c * P + k] = G[(2 * c + 1) * P + k] + G[(2 * c + 2) * P + k];
+        int64_t c = start + e / S;
+        int k = (int)(e % S);
+        G[c * S + k] = G[(2 * c + 1) * S + k] + G[(2 * c + 2) * S + k];
     }
 }
 
 template <typename T>
 __global__ void tree_scale_kernel(const T *__restrict__ src, T *__restrict__ dst, int64_t total,
-                                  int P, const double *__restrict__ mat) {
+                                  int P, int S, const double *__restrict__ mat) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        dst[e] = (T)((double)src[e] * mat[e % P]);
+        int k = (int)(e % S);
+        dst[e] = k < P ? (T)((double)src[e] * mat[k]) : T(0);
     }
 }
 
@@ -169,9 +174,10 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     int64_t end = geom.node_count - geom.leaf_count;
     while (true) {
         if (end > start) {
-            int64_t total = (end - start) * (int64_t)P;
+            const int S = node_stride(R, sizeof(T));
+            int64_t total = (end - start) * (int64_t)S;
             int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
-            level_sum_kernel<T><<<blocks, 256, 0, st>>>(G, start, end, P);
+            level_sum_kernel<T><<<blocks, 256, 0, st>>>(G, start, end, S);
             rc = check_launch("level_sum_kernel");
             if (rc) return rc;
         }
@@ -210,7 +216,8 @@ extern "C" int ftl_tree_bytes(int64_t n, int64_t F, int R, int prec, size_t *out
                   "ftl_tree_bytes: bad shape n=%lld F=%lld R=%d", (long long)n, (long long)F, R);
     FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_tree_bytes: bad precision %d", prec);
     Geom g = make_geom(n, F);
-    *out_bytes = (size_t)g.node_count * packed_size(R) * (prec == FTL_PREC_FP64 ? 8 : 4);
+    const int esize = prec == FTL_PREC_FP64 ? 8 : 4;
+    *out_bytes = (size_t)g.node_count * node_stride(R, esize) * esize;
     return FTL_OK;
 }
 
@@ -230,15 +237,15 @@ extern "C" int ftl_tree_scale(const void *G_src, void *G_dst, int64_t node_count
                               const double *mat, void *stream) {
     FTL_CHECK_ARG(G_src && G_dst && mat, "ftl_tree_scale: null pointer");
     FTL_CHECK_ARG(node_count >= 1 && R >= 1 && R <= FTL_MAX_RANK, "ftl_tree_scale: bad shape");
+    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_tree_scale: bad precision %d", prec);
     const int P = packed_size(R);
-    int64_t total = node_count * (int64_t)P;
+    const int S = node_stride(R, prec == FTL_PREC_FP64 ? 8 : 4);
+    int64_t total = node_count * (int64_t)S;
     int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
     cudaStream_t st = (cudaStream_t)stream;
     if (prec == FTL_PREC_FP64)
-        tree_scale_kernel<double><<<blocks, 256, 0, st>>>((const double *)G_src, (double *)G_dst, total, P, mat);
-    else if (prec == FTL_PREC_FP32)
-        tree_scale_kernel<float><<<blocks, 256, 0, st>>>((const float *)G_src, (float *)G_dst, total, P, mat);
+        tree_scale_kernel<double><<<blocks, 256, 0, st>>>((const double *)G_src, (double *)G_dst, total, P, S, mat);
     else
-        return fail(FTL_E_ARG, "ftl_tree_scale: bad precision %d", prec);
+        tree_scale_kernel<float><<<blocks, 256, 0, st>>>((const float *)G_src, (float *)G_dst, total, P, S, mat);
     return check_launch("tree_scale_kernel");
 }

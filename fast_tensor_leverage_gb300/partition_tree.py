@@ -31,7 +31,9 @@ class PartitionTree:
         self.lfill_level = g.lfill_level
         self.P = R * (R + 1) // 2
         dt = torch.float64 if precision == "fp64" else torch.float32
-        self.G = torch.zeros(self.node_count * self.P, dtype=dt, device=self.device)
+        nbytes = _lib.tree_bytes(n, F, R, self._prec)
+        self.S = nbytes // (self.node_count * dt.itemsize)  # node stride (16-byte padded)
+        self.G = torch.zeros(nbytes // dt.itemsize, dtype=dt, device=self.device)
         self._G_unmultiplied = None
         self._U = None
 
@@ -68,7 +70,7 @@ class PartitionTree:
 
     def get_G(self) -> np.ndarray:
         """All node Grams as packed upper triangles, (node_count, P)."""
-        return self.G.double().cpu().numpy().reshape(self.node_count, self.P)
+        return self.G.double().cpu().numpy().reshape(self.node_count, self.S)[:, : self.P].copy()
 
     def PTSample(self, U, h, scaled_h, samples, random_draws) -> None:
         """PartitionTree::PTSample (partition_tree.hpp:216-405): for every row

@@ -189,12 +189,19 @@ class Sampler:
     def weights(self) -> np.ndarray:
         return self.weights_dev.cpu().numpy()
 
+    def _stride(self) -> int:
+        w = 16 // (8 if self.precision == "fp64" else 4)
+        return (self.P + w - 1) // w * w
+
     def gram_tree(self, k: int) -> np.ndarray:
         """Node Grams of factor k's tree, (node_count, P) packed, as FP64."""
-        return self.trees[k].double().cpu().numpy().reshape(-1, self.P)
+        S = self._stride()
+        return self.trees[k].double().cpu().numpy().reshape(-1, S)[:, : self.P].copy()
 
     def eigen_tree(self, k: int) -> np.ndarray:
-        return self.eig_G.double().cpu().numpy().reshape(self.N, 2 * self.R - 1, self.P)[k]
+        S = self._stride()
+        e = self.eig_G.double().cpu().numpy().reshape(self.N, 2 * self.R - 1, S)
+        return e[k, :, : self.P].copy()
 
     def workspace_M(self) -> np.ndarray:
         return self.M.cpu().numpy().reshape(-1, self.R, self.R)
