@@ -40,14 +40,15 @@ __device__ __forceinline__ double root_at(const CMParams &p, int k, int e) {
     return (double)((const float *)p.root[k])[e];
 }
 
-// In-place Jacobi on A (R x R, symmetric, row-major); V receives the
-// eigenvectors as columns; lam_rank[v] gets the ascending rank of eigenvalue v.
-// All threads of the block must call it.
-__device__ void jacobi_eigen(double *A, double *V, int R, double *csbuf, int *pqbuf, int *flag) {
+// In-place Jacobi on A (R x R, symmetric, row-major, element type T); V
+// receives the eigenvectors as columns.  All threads of the block must call it.
+template <typename T>
+__device__ void jacobi_eigen(T *A, T *V, int R, T *csbuf, int *pqbuf, int *flag) {
     const int tid = threadIdx.x, nth = blockDim.x;
     const int n = R + (R & 1);
     const int half = n / 2;
-    for (int e = tid; e < R * R; e += nth) V[e] = (e / R == e % R) ? 1.0 : 0.0;
+    const T eps = sizeof(T) == 8 ? T(1.1102230246251565e-16) : T(5.9604645e-08);
+    for (int e = tid; e < R * R; e += nth) V[e] = (e / R == e % R) ? T(1) : T(0);
     __syncthreads();
     for (int sweep = 0; sweep < 40; ++sweep) {
         if (tid == 0) *flag = 0;
@@ -67,19 +68,19 @@ __device__ void jacobi_eigen(double *A, double *V, int R, double *csbuf, int *pq
                     p = q;
                     q = t;
                 }
-                double c = 1.0, s = 0.0;
+                T c = T(1), s = T(0);
                 if (q < R) {
-                    double apq = A[p * R + q];
-                    double app = A[p * R + p];
-                    double aqq = A[q * R + q];
-                    if (apq != 0.0 && fabs(apq) > 1.1102230246251565e-16 * sqrt(fabs(app * aqq))) {
-                        double theta = (aqq - app) / (2.0 * apq);
-                        double t;
-                        if (fabs(theta) > 1e150)
-                            t = 0.5 / theta;
+                    T apq = A[p * R + q];
+                    T app = A[p * R + p];
+                    T aqq = A[q * R + q];
+                    if (apq != T(0) && fabs(apq) > eps * sqrt(fabs(app * aqq))) {
+                        T theta = (aqq - app) / (T(2) * apq);
+                        T t;
+                        if (fabs(theta) > T(sizeof(T) == 8 ? 1e150 : 1e18))
+                            t = T(0.5) / theta;
                         else
-                            t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
-                        c = 1.0 / sqrt(1.0 + t * t);
+                            t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(T(1) + theta * theta));
+                        c = T(1) / sqrt(T(1) + t * t);
                         s = t * c;
                         *flag = 1;
                     }
@@ -93,14 +94,14 @@ __device__ void jacobi_eigen(double *A, double *V, int R, double *csbuf, int *pq
             // A <- A J and V <- V J (columns p, q of each rotated pair)
             for (int w = tid; w < half * R; w += nth) {
                 int i = w / R, r = w - i * R;
-                double s = csbuf[2 * i + 1];
-                if (s == 0.0) continue;
-                double c = csbuf[2 * i];
+                T s = csbuf[2 * i + 1];
+                if (s == T(0)) continue;
+                T c = csbuf[2 * i];
                 int p = pqbuf[2 * i], q = pqbuf[2 * i + 1];
-                double arp = A[r * R + p], arq = A[r * R + q];
+                T arp = A[r * R + p], arq = A[r * R + q];
                 A[r * R + p] = c * arp - s * arq;
                 A[r * R + q] = s * arp + c * arq;
-                double vrp = V[r * R + p], vrq = V[r * R + q];
+                T vrp = V[r * R + p], vrq = V[r * R + q];
                 V[r * R + p] = c * vrp - s * vrq;
                 V[r * R + q] = s * vrp + c * vrq;
             }
@@ -108,21 +109,21 @@ __device__ void jacobi_eigen(double *A, double *V, int R, double *csbuf, int *pq
             // A <- J^T A (rows p, q)
             for (int w = tid; w < half * R; w += nth) {
                 int i = w / R, col = w - i * R;
-                double s = csbuf[2 * i + 1];
-                if (s == 0.0) continue;
-                double c = csbuf[2 * i];
+                T s = csbuf[2 * i + 1];
+                if (s == T(0)) continue;
+                T c = csbuf[2 * i];
                 int p = pqbuf[2 * i], q = pqbuf[2 * i + 1];
-                double apc = A[p * R + col], aqc = A[q * R + col];
+                T apc = A[p * R + col], aqc = A[q * R + col];
                 A[p * R + col] = c * apc - s * aqc;
                 A[q * R + col] = s * apc + c * aqc;
             }
             __syncthreads();
             if (tid < half) {
-                double s = csbuf[2 * tid + 1];
-                if (s != 0.0) {
+                T s = csbuf[2 * tid + 1];
+                if (s != T(0)) {
                     int p = pqbuf[2 * tid], q = pqbuf[2 * tid + 1];
-                    A[p * R + q] = 0.0;
-                    A[q * R + p] = 0.0;
+                    A[p * R + q] = T(0);
+                    A[q * R + p] = T(0);
                 }
             }
             __syncthreads();
@@ -134,17 +135,48 @@ __device__ void jacobi_eigen(double *A, double *V, int R, double *csbuf, int *pq
 }
 
 // order[r] = index of the r-th smallest eigenvalue (ties by index).
-__device__ void sort_ascending(const double *A, int R, int *order) {
+template <typename T>
+__device__ void sort_ascending(const T *A, int R, int *order) {
     for (int v = threadIdx.x; v < R; v += blockDim.x) {
-        double lv = A[v * R + v];
+        T lv = A[v * R + v];
         int rank = 0;
         for (int u = 0; u < R; ++u) {
-            double lu = A[u * R + u];
+            T lu = A[u * R + u];
             if (lu < lv || (lu == lv && u < v)) ++rank;
         }
         order[rank] = v;
     }
     __syncthreads();
+}
+
+// In-place lower Cholesky factor of (A - shift I), A dense R x R FP64 in
+// shared memory (lower triangle used).  Returns true (block-uniformly) when
+// every pivot is positive, i.e. A - shift I is positive definite.
+__device__ bool cholesky_lower(double *A, int R, double shift, int *flag) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    if (tid == 0) *flag = 1;
+    for (int e = tid; e < R; e += nth) A[e * R + e] -= shift;
+    __syncthreads();
+    for (int k = 0; k < R; ++k) {
+        if (tid == 0) {
+            double d = A[k * R + k];
+            if (!(d > 0.0)) *flag = 0;
+            A[k * R + k] = d > 0.0 ? sqrt(d) : 1.0;
+        }
+        __syncthreads();
+        if (*flag == 0) break;
+        const double lkk = A[k * R + k];
+        for (int i = k + 1 + tid; i < R; i += nth) A[i * R + k] /= lkk;
+        __syncthreads();
+        const int m = R - k - 1;
+        for (int w = tid; w < m * m; w += nth) {
+            int i = k + 1 + w / m, jj = k + 1 + w % m;
+            if (jj <= i) A[i * R + jj] -= A[i * R + k] * A[jj * R + k];
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    return *flag != 0;
 }
 
 // Shared memory: A (R*R), V (R*R unless kept in global scratch), cs (R+2),
@@ -182,10 +214,51 @@ __global__ void computem_pinv_kernel(CMParams p) {
         for (int e = tid; e < RR; e += nth) p.M[e] = p.M[(size_t)RR + e];
         __syncthreads();
     }
+    double *status = p.M + (size_t)(2 * N + 3) * RR;  // 1.0: Cholesky path taken
+    bool chol = false;
+    if (p.prec == FTL_PREC_FP32) {
+        // Mixed mode: when every eigenvalue of M[0] exceeds the reference's
+        // 1e-8 cut (M[0] - 1e-8 I positive definite), its pseudo-inverse is
+        // the inverse, computed in FP64 from the Cholesky factor:
+        // pinv = L^-T L^-1.  Otherwise the Jacobi path below runs.
+        for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
+        __syncthreads();
+        chol = cholesky_lower(A, R, 1e-8, flag);
+        if (chol) {
+            for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
+            __syncthreads();
+            chol = cholesky_lower(A, R, 0.0, flag);
+        }
+        if (chol) {
+            // V = L^-1 (lower), one column per thread, forward substitution
+            for (int jc = tid; jc < R; jc += nth) {
+                for (int i = 0; i < R; ++i) {
+                    double y = 0.0;
+                    if (i >= jc) {
+                        double acc = (i == jc) ? 1.0 : 0.0;
+                        for (int kk = jc; kk < i; ++kk) acc -= A[i * R + kk] * V[kk * R + jc];
+                        y = acc / A[i * R + i];
+                    }
+                    V[i * R + jc] = y;
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < RR; e += nth) {
+                int a = e / R, b = e - a * R;
+                int lo = max(a, b);
+                double acc = 0.0;
+                for (int kk = lo; kk < R; ++kk) acc += V[kk * R + a] * V[kk * R + b];
+                A[e] = acc;  // A is free again: the factor is no longer needed after this pass
+            }
+            __syncthreads();
+        }
+    }
+    if (tid == 0) *status = chol ? 1.0 : 0.0;
+    if (!chol) {
     for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
     __syncthreads();
-    jacobi_eigen(A, V, R, cs, pq, flag);
-    sort_ascending(A, R, order);
+    jacobi_eigen<double>(A, V, R, cs, pq, flag);
+    sort_ascending<double>(A, R, order);
     // W = M[N]: row (R-1-r) = v_r / sqrt(lambda_r) for lambda_r > 1e-8, else 0,
     // r the ascending rank (column R-1-r of the reference's V Lambda^{-1/2}).
     double *W = p.M + (size_t)N * RR;
@@ -209,6 +282,7 @@ __global__ void computem_pinv_kernel(CMParams p) {
         A[e] = acc;
     }
     __syncthreads();
+    }
     double *pinv_packed = p.M + (size_t)(N + 1) * RR;
     for (int e = tid; e < RR; e += nth) {
         p.M[e] = A[e];
@@ -243,11 +317,38 @@ __global__ void computem_eig_kernel(CMParams p) {
     int *flag = order + R;
     const int offset = ((uint32_t)(k + 1) == p.j) ? k + 2 : k + 1;
     double *W = p.M + (size_t)offset * RR;
-    if (offset < N) {
+    const bool chol = p.M[(size_t)(2 * N + 3) * RR] == 1.0;
+    if (p.prec == FTL_PREC_FP32 && (offset < N || chol)) {
+        // Mixed mode: FP32 Jacobi of M[offset] (offset < N), or of the FP64
+        // pseudo-inverse when it came from the Cholesky path (offset == N;
+        // its eigenvectors are those of M[0], its eigenvalues 1/lambda, so
+        // ascending order here is the reference's descending-lambda order of
+        // the rows lambda^-1/2 v^T).  Rows sqrt(mu_r) v_r, ascending mu_r.
+        float *A32 = (float *)smem_raw;
+        float *V32 = A32 + RR;
+        float *cs32 = V32 + RR;
+        int *pq32 = (int *)(cs32 + R + 2);
+        int *order32 = pq32 + R + 2;
+        int *flag32 = order32 + R;
+        const double *src = offset < N ? W : p.M;  // M[0] holds the full pseudo-inverse
+        for (int e = tid; e < RR; e += nth) A32[e] = (float)src[e];
+        __syncthreads();
+        jacobi_eigen<float>(A32, V32, R, cs32, pq32, flag32);
+        sort_ascending<float>(A32, R, order32);
+        for (int e = tid; e < RR; e += nth) {
+            int r = e / R, a = e - r * R;
+            int v = order32[r];
+            float lam = A32[v * R + v];
+            W[e] = (double)(sqrtf(fmaxf(lam, 0.0f)) * V32[a * R + v]);
+        }
+        for (int r = tid; r < R; r += nth)
+            p.lambda[(size_t)offset * R + r] = (double)A32[order32[r] * R + order32[r]];
+        __syncthreads();
+    } else if (offset < N) {
         for (int e = tid; e < RR; e += nth) A[e] = W[e];
         __syncthreads();
-        jacobi_eigen(A, V, R, cs, pq, flag);
-        sort_ascending(A, R, order);
+        jacobi_eigen<double>(A, V, R, cs, pq, flag);
+        sort_ascending<double>(A, R, order);
         // row r = sqrt(lambda_r) v_r, ascending (negative rounding noise -> 0)
         for (int e = tid; e < RR; e += nth) {
             int r = e / R, a = e - r * R;

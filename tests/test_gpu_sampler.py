@@ -123,6 +123,7 @@ def test_philox_stream_equals_injected_oracle_uniforms(ftl):
     (4, [1000] * 4, 8, 10000, 5),
     (3, [4096, 2048, 3000], 32, 4000, 1),
     (2, [5000, 3000], 64, 2000, 3),
+    (3, [20, 30, 40], 32, 3000, 4),   # rank-deficient Grams: Jacobi pseudo-inverse path
 ])
 def test_fp32_draw_agrees_with_fp64_oracle(ftl, N, dims, R, J, j):
     rng = np.random.default_rng(31 + R)
