@@ -149,14 +149,63 @@ struct QForm {
         }
         return warp_sum(acc);
     }
+
+    // Two independent forms with interleaved loads (one memory round trip).
+    __device__ __forceinline__ void eval2(const T *__restrict__ na, const T *__restrict__ nb,
+                                          int lane, T &ra, T &rb) const {
+        T acc_a = T(0), acc_b = T(0);
+        if (S_::XX_SMEM) {
+#pragma unroll 2
+            for (int e = lane * W; e < S; e += 32 * W) {
+                V ga = __ldg(reinterpret_cast<const V *>(na + e));
+                V gb = __ldg(reinterpret_cast<const V *>(nb + e));
+                V x = *reinterpret_cast<const V *>(s + e);
+                T av[W], bv[W], xv[W];
+                Vec16<T>::get(ga, av);
+                Vec16<T>::get(gb, bv);
+                Vec16<T>::get(x, xv);
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    acc_a = fma(av[w], xv[w], acc_a);
+                    acc_b = fma(bv[w], xv[w], acc_b);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int t = 0; t < NS::NV; ++t) {
+                int e = (lane + 32 * t) * W;
+                if (e < S) {
+                    V ga = __ldg(reinterpret_cast<const V *>(na + e));
+                    V gb = __ldg(reinterpret_cast<const V *>(nb + e));
+                    T av[W], bv[W];
+                    Vec16<T>::get(ga, av);
+                    Vec16<T>::get(gb, bv);
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        acc_a = fma(av[w], r[t * W + w], acc_a);
+                        acc_b = fma(bv[w], r[t * W + w], acc_b);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc_a += __shfl_xor_sync(0xffffffffu, acc_a, o);
+            acc_b += __shfl_xor_sync(0xffffffffu, acc_b, o);
+        }
+        ra = acc_a;
+        rb = acc_b;
+    }
 };
 
-// L2 prefetch of `bytes` bytes at p, spread over the warp's lanes.
-__device__ __forceinline__ void prefetch_l2(const void *p, int bytes, int lane) {
-    const char *c = (const char *)p;
-    for (int off = lane * 128; off < bytes; off += 32 * 128)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(c + off));
-    if (lane == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + bytes - 1));
+// L2 prefetch of the 128-byte lines covering [p, p + bytes), one line per
+// lane per pass.  Every address issued is the start of a line that holds at
+// least one byte of the range, so it lies inside the range's allocation.
+__device__ __forceinline__ void prefetch_lines(const void *p, int64_t bytes, int lane) {
+    const uintptr_t a0 = (uintptr_t)p & ~(uintptr_t)127;
+    const uintptr_t a1 = ((uintptr_t)p + (uintptr_t)bytes - 1) & ~(uintptr_t)127;
+    for (uintptr_t a = a0 + 128 * (uintptr_t)lane; a <= a1; a += 32 * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
 }
 
 // Before evaluating level `c` -> child 2c+1, fetch into L2 what the next step
@@ -165,16 +214,24 @@ __device__ __forceinline__ void prefetch_l2(const void *p, int bytes, int lane) 
 template <typename T>
 __device__ __forceinline__ void prefetch_next(const T *G, int S, const DGeom &g, int64_t c,
                                               const double *U, int R, int lane) {
+    const int64_t c1 = 2 * c + 1;
+    if (!is_leaf(g, c1 + 1)) {
+        // both children internal: their left children are adjacent pairs
+        // 2c1+1 and 2c1+3 -> two node ranges
+        prefetch_lines(G + (2 * c1 + 1) * (int64_t)S, (int64_t)S * sizeof(T), lane);
+        prefetch_lines(G + (2 * c1 + 3) * (int64_t)S, (int64_t)S * sizeof(T), lane);
+        return;
+    }
 #pragma unroll
-    for (int side = 1; side <= 2; ++side) {
-        const int64_t cc = 2 * c + side;
+    for (int side = 0; side < 2; ++side) {
+        const int64_t cc = c1 + side;
         if (cc >= g.node_count) continue;
         if (!is_leaf(g, cc)) {
-            prefetch_l2(G + (2 * cc + 1) * (int64_t)S, S * (int)sizeof(T), lane);
+            prefetch_lines(G + (2 * cc + 1) * (int64_t)S, (int64_t)S * sizeof(T), lane);
         } else if (U != nullptr) {
             const int64_t row0 = leaf_index(g, cc) * g.F;
             const int64_t rows = min(g.F, g.n - row0);
-            prefetch_l2(U + row0 * R, (int)(rows * R * (int64_t)sizeof(double)), lane);
+            prefetch_lines(U + row0 * R, rows * R * (int64_t)sizeof(double), lane);
         }
     }
 }
@@ -187,11 +244,23 @@ __device__ __forceinline__ int64_t descend(const double *__restrict__ G, int S, 
                                            double &frac, const double *U = nullptr, int R = 0) {
     int64_t c = 0;
     double low = 0.0, high = 1.0;
-    if (!is_leaf(g, 0)) prefetch_l2(G + S, S * 8, lane);
-    const double m = qf.eval(G, lane);
+    if (is_leaf(g, 0)) {  // single-leaf tree: the leaf fraction is the draw
+        frac = draw;
+        return 0;
+    }
+    // the root mass and the first left-child mass need no decision between
+    // them: one round trip for both
+    prefetch_next(G, S, g, 0, U, R, lane);
+    double m, mL0;
+    qf.eval2(G, G + S, lane, m, mL0);
     for (int64_t lvl = 0; lvl < g.lfill_level; ++lvl) {
-        prefetch_next(G, S, g, c, U, R, lane);
-        double mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
+        double mL;
+        if (lvl == 0) {
+            mL = mL0;
+        } else {
+            prefetch_next(G, S, g, c, U, R, lane);
+            mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
+        }
         double cutoff = low + mL / m;
         if (draw <= cutoff) {
             c = 2 * c + 1;
@@ -235,16 +304,26 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
                                            double draw, const QForm<RMAX, float> &qf, int lane,
                                            float &frac, const double *U = nullptr, int R = 0) {
     int64_t c = 0;
-    if (!is_leaf(g, 0)) prefetch_l2(G + S, S * 4, lane);
-    float mP = qf.eval(G, lane);
+    if (is_leaf(g, 0)) {  // single-leaf tree: the leaf fraction is the draw
+        frac = (float)draw;
+        return 0;
+    }
+    prefetch_next(G, S, g, 0, U, R, lane);
+    float mP, mL0;
+    qf.eval2(G, G + S, lane, mP, mL0);
     double t0 = draw * (double)mP;
     float th = (float)t0;
     float tl = (float)(t0 - (double)th);
     int64_t steps = g.lfill_level + 1;
     for (int64_t lvl = 0; lvl < steps; ++lvl) {
         if (lvl == g.lfill_level && is_leaf(g, c)) break;
-        prefetch_next(G, S, g, c, U, R, lane);
-        float mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
+        float mL;
+        if (lvl == 0) {
+            mL = mL0;
+        } else {
+            prefetch_next(G, S, g, c, U, R, lane);
+            mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
+        }
         bool left = ((th - mL) + tl) <= 0.0f;
         if (left) {
             c = 2 * c + 1;

@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
     qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
     const size_t RR = (size_t)R * R;
     const size_t eig_stride = (size_t)(2 * R - 1) * p.S;
+    const float RJ = (float)((double)R / (double)p.J);
 
     for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
          i += (int64_t)gridDim.x * S::WARPS) {
@@ -105,13 +106,15 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 102
         if (p.weights) {
             double scale = stage_query<RMAX, T>(h, R, xd, xT, lane);
             qf.setup(xT, pairs, lane);
-            double lev;
             if (sizeof(T) == 8) {
-                lev = (double)qf.eval((const T *)(p.M + (size_t)(p.N + 1) * RR), lane);
+                double lev = (double)qf.eval((const T *)(p.M + (size_t)(p.N + 1) * RR), lane);
+                if (lane == 0) p.weights[i] = (double)R / (lev * (double)p.J);
             } else {
-                lev = (double)qf.eval((const T *)p.pinv32, lane) / (scale * scale);
+                // w = R / (J lev), lev = lev_scaled / scale^2: the quotient in
+                // FP32, the power-of-two rescale as one exact FP64 product
+                float lev_s = (float)qf.eval((const T *)p.pinv32, lane);
+                if (lane == 0) p.weights[i] = (double)(RJ / lev_s) * (scale * scale);
             }
-            if (lane == 0) p.weights[i] = (double)R / (lev * (double)p.J);
         }
         if (p.h) {
 #pragma unroll
