@@ -50,16 +50,22 @@ def _needs_rebuild() -> bool:
     return any(p.stat().st_mtime > t for p in deps if p.exists())
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    if not force and not _needs_rebuild():
+def build(force: bool = False, verbose: bool = False, defines: list[str] | None = None,
+          out: Path | None = None) -> Path:
+    """Compile and link.  `defines` (e.g. ["FTL_DESC_PREFETCH=0"]) and `out`
+    build a tuning variant of the library next to the default one."""
+    lib_path = Path(out) if out is not None else LIB
+    if not force and defines is None and out is None and not _needs_rebuild():
         return LIB
-    BUILD.mkdir(parents=True, exist_ok=True)
+    build_dir = lib_path.parent / (lib_path.stem + "_obj") if out is not None else BUILD
+    build_dir.mkdir(parents=True, exist_ok=True)
+    extra = [f"-D{d}" for d in (defines or [])]
     cc = nvcc()
     objs = []
 
     def compile_one(src: Path) -> Path:
-        obj = BUILD / (src.stem + ".o")
-        cmd = [cc, *NVCC_FLAGS, "-I", str(PKG.parent / "include"), "-c", str(src), "-o", str(obj)]
+        obj = build_dir / (src.stem + ".o")
+        cmd = [cc, *NVCC_FLAGS, *extra, "-I", str(PKG.parent / "include"), "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)
@@ -72,13 +78,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = BUILD / (LIB.name + ".tmp")
+    tmp = build_dir / (lib_path.name + ".tmp")
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

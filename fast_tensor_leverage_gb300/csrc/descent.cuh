@@ -22,6 +22,20 @@
 
 #include "ftl_common.cuh"
 
+// Compile-time tuning knobs (defaults are the measured best on GB300).
+#ifndef FTL_DESC_PREFETCH
+#define FTL_DESC_PREFETCH 1        // L2 prefetch of next-level candidates
+#endif
+#ifndef FTL_DESC_WARPS32
+#define FTL_DESC_WARPS32 8         // warps per block for R <= 32
+#endif
+#ifndef FTL_DESC_RESIDENT_F32
+#define FTL_DESC_RESIDENT_F32 1024 // threads per SM the FP32 kernels are register-budgeted for
+#endif
+#ifndef FTL_DESC_RESIDENT_F64
+#define FTL_DESC_RESIDENT_F64 512
+#endif
+
 namespace ftl {
 
 template <int RMAX>
@@ -30,7 +44,7 @@ struct Shape {
     static constexpr int XPL = (RMAX + 31) / 32;  // vector entries per lane
     static constexpr int FQ = (RMAX + 31) / 32;   // leaf rows per lane (F <= R)
     static constexpr bool XX_SMEM = RMAX > 32;
-    static constexpr int WARPS = RMAX <= 32 ? 8 : (RMAX <= 64 ? 4 : 2);
+    static constexpr int WARPS = RMAX <= 32 ? FTL_DESC_WARPS32 : (RMAX <= 64 ? 4 : 2);
 };
 
 // 16-byte vector of the tree precision.
@@ -214,6 +228,7 @@ __device__ __forceinline__ void prefetch_lines(const void *p, int64_t bytes, int
 template <typename T>
 __device__ __forceinline__ void prefetch_next(const T *G, int S, const DGeom &g, int64_t c,
                                               const double *U, int R, int lane) {
+    if (!FTL_DESC_PREFETCH) return;
     const int64_t c1 = 2 * c + 1;
     if (!is_leaf(g, c1 + 1)) {
         // both children internal: their left children are adjacent pairs

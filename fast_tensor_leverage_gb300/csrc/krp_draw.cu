@@ -42,7 +42,7 @@ __device__ __forceinline__ double get_draw(const DrawParams &p, int64_t idx) {
 }
 
 template <int RMAX, typename T>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 1024 : 512) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -142,7 +142,7 @@ struct TreeSampleParams {
 // PartitionTree::PTSample_internal (cpp_ext/partition_tree.hpp:232-405):
 // x = scaled_h[i]; samples[i] = selected row; h[i] o= U[row].
 template <int RMAX, typename T>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? 1024 : 512) / (Shape<RMAX>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
