@@ -24,7 +24,16 @@
 
 // Compile-time tuning knobs (defaults are the measured best on GB300).
 #ifndef FTL_DESC_PREFETCH
-#define FTL_DESC_PREFETCH 1        // L2 prefetch of next-level candidates
+#define FTL_DESC_PREFETCH 0        // L2 prefetch of next-level candidates (measured slower)
+#endif
+#ifndef FTL_DESC_XX_SMEM32
+#define FTL_DESC_XX_SMEM32 0       // keep the outer product in shared memory also for R <= 32
+#endif
+#ifndef FTL_DESC_EVAL2
+#define FTL_DESC_EVAL2 1           // root and first-level forms in one round trip
+#endif
+#ifndef FTL_DESC_LEAF_CHUNK
+#define FTL_DESC_LEAF_CHUNK 32     // leaf rows loaded per round trip (8, 16 or 32)
 #endif
 #ifndef FTL_DESC_WARPS32
 #define FTL_DESC_WARPS32 8         // warps per block for R <= 32
@@ -43,7 +52,7 @@ struct Shape {
     static constexpr int PMAX = RMAX * (RMAX + 1) / 2;
     static constexpr int XPL = (RMAX + 31) / 32;  // vector entries per lane
     static constexpr int FQ = (RMAX + 31) / 32;   // leaf rows per lane (F <= R)
-    static constexpr bool XX_SMEM = RMAX > 32;
+    static constexpr bool XX_SMEM = RMAX > 32 || FTL_DESC_XX_SMEM32;
     static constexpr int WARPS = RMAX <= 32 ? FTL_DESC_WARPS32 : (RMAX <= 64 ? 4 : 2);
 };
 
@@ -138,15 +147,18 @@ struct QForm {
     __device__ __forceinline__ T eval(const T *__restrict__ node, int lane) const {
         T acc = T(0);
         if (S_::XX_SMEM) {
-#pragma unroll 2
-            for (int e = lane * W; e < S; e += 32 * W) {
-                V g = __ldg(reinterpret_cast<const V *>(node + e));
-                V x = *reinterpret_cast<const V *>(s + e);
-                T gv[W], xv[W];
-                Vec16<T>::get(g, gv);
-                Vec16<T>::get(x, xv);
+#pragma unroll(NS::NV <= 8 ? NS::NV : 2)
+            for (int t = 0; t < NS::NV; ++t) {
+                int e = (lane + 32 * t) * W;
+                if (e < S) {
+                    V g = __ldg(reinterpret_cast<const V *>(node + e));
+                    V x = *reinterpret_cast<const V *>(s + e);
+                    T gv[W], xv[W];
+                    Vec16<T>::get(g, gv);
+                    Vec16<T>::get(x, xv);
 #pragma unroll
-                for (int w = 0; w < W; ++w) acc = fma(gv[w], xv[w], acc);
+                    for (int w = 0; w < W; ++w) acc = fma(gv[w], xv[w], acc);
+                }
             }
         } else {
 #pragma unroll
@@ -267,7 +279,12 @@ __device__ __forceinline__ int64_t descend(const double *__restrict__ G, int S, 
     // them: one round trip for both
     prefetch_next(G, S, g, 0, U, R, lane);
     double m, mL0;
-    qf.eval2(G, G + S, lane, m, mL0);
+    if (FTL_DESC_EVAL2) {
+        qf.eval2(G, G + S, lane, m, mL0);
+    } else {
+        m = qf.eval(G, lane);
+        mL0 = qf.eval(G + S, lane);
+    }
     for (int64_t lvl = 0; lvl < g.lfill_level; ++lvl) {
         double mL;
         if (lvl == 0) {
@@ -325,7 +342,12 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
     }
     prefetch_next(G, S, g, 0, U, R, lane);
     float mP, mL0;
-    qf.eval2(G, G + S, lane, mP, mL0);
+    if (FTL_DESC_EVAL2) {
+        qf.eval2(G, G + S, lane, mP, mL0);
+    } else {
+        mP = qf.eval(G, lane);
+        mL0 = qf.eval(G + S, lane);
+    }
     double t0 = draw * (double)mP;
     float th = (float)t0;
     float tl = (float)(t0 - (double)th);
@@ -373,19 +395,29 @@ __device__ __forceinline__ LaneQuery<RMAX, T> lane_query(const T *x, int R, int 
     return q;
 }
 
-// Sum over lanes of 32 per-lane values at once: afterwards lane l holds
-// sum_lanes v[l] in v[0] (butterfly that halves the live values per stage,
-// 31 shuffles instead of 32 x 5).
-template <typename T>
-__device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
+// Sum over lanes of K per-lane values at once (K = 8, 16 or 32): a butterfly
+// that halves the live values per stage, then plain adds.  Afterwards lane l
+// holds in v[0] the warp-wide sum of value index (l >> (5 - log2 K)).
+template <int K, typename T>
+__device__ __forceinline__ T transpose_reduce(T (&v)[K], int lane) {
+    static_assert(K == 8 || K == 16 || K == 32, "K must be 8, 16 or 32");
+    int live = K;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
-        const bool upper = (lane & off) != 0;
+        if (live > 1) {
+            const int h = live / 2;
+            const bool upper = (lane & off) != 0;
 #pragma unroll
-        for (int i = 0; i < off; ++i) {
-            T send = upper ? v[i] : v[i + off];
-            T keep = upper ? v[i + off] : v[i];
-            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+            for (int i = 0; i < K / 2; ++i) {
+                if (i < h) {
+                    T send = upper ? v[i] : v[i + h];
+                    T keep = upper ? v[i + h] : v[i];
+                    v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+                }
+            }
+            live = h;
+        } else {
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
         }
     }
     return v[0];
@@ -393,29 +425,31 @@ __device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
 
 // Row selection inside leaf block c (F > 1): q_r = U[row0+r] . x for the
 // block's rows, inclusive prefix of q_r^2 in row order, first r <= F-2 with
-// frac < prefix_r / total, else F-1.  The block is read row by row with
-// coalesced loads (lane = column), all issued before any use, and the 32 row
-// dot products are finished by one transpose-reduce.  xq holds the warp's
-// query in the compute type.  A selection past
-// the last row of a partial block (only reachable when frac rounds to >= 1)
-// is clamped to that last row.
+// frac < prefix_r / total, else F-1.  The block is read in chunks of K rows
+// with coalesced loads (lane = column), all loads of a chunk issued before
+// any use, and each chunk's K row dot products are finished by one
+// transpose-reduce.  xq holds the warp's query in the compute type.  A
+// selection past the last row of a partial block (only reachable when frac
+// rounds to >= 1) is clamped to that last row.
 template <int RMAX, typename T>
 __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R, const DGeom &g,
                                              int64_t c, T frac, const LaneQuery<RMAX, T> &xq,
                                              int lane) {
-    constexpr int FQ = Shape<RMAX>::FQ;
     constexpr int XPL = Shape<RMAX>::XPL;
+    constexpr int K = FTL_DESC_LEAF_CHUNK;
+    constexpr int LOGK = K == 8 ? 3 : (K == 16 ? 4 : 5);
+    constexpr int NCH = (RMAX + K - 1) / K;  // chunks covering F <= RMAX rows
     const int64_t leaf = leaf_index(g, c);
     const int F = (int)g.F;
     const int64_t row0 = leaf * g.F;
     const int rows = (int)min((int64_t)F, g.n - row0);
-    T q2[FQ];
+    T q2[NCH];
 #pragma unroll
-    for (int qi = 0; qi < FQ; ++qi) {
-        T v[32];
+    for (int ch = 0; ch < NCH; ++ch) {
+        T v[K];
 #pragma unroll
-        for (int rr = 0; rr < 32; ++rr) {
-            const int r = 32 * qi + rr;
+        for (int rr = 0; rr < K; ++rr) {
+            const int r = K * ch + rr;
             T acc = T(0);
             if (r < rows) {
                 const double *u = U + (row0 + r) * (int64_t)R;
@@ -427,22 +461,25 @@ __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R
             }
             v[rr] = acc;
         }
-        T q = transpose_reduce32<T>(v, lane);
-        q2[qi] = q * q;
+        T q = transpose_reduce<K, T>(v, lane);
+        q2[ch] = q * q;
     }
+    // Sequential prefix in row order (same association as the reference's
+    // running sum); every lane walks the same sequence, lane r keeps row r's
+    // prefix (rows >= 32 in the further slots).
+    constexpr int FQ = Shape<RMAX>::FQ;
     T incl[FQ];
-    T run = T(0);
 #pragma unroll
     for (int qi = 0; qi < FQ; ++qi) incl[qi] = T(0);
-    // Sequential prefix in row order (same association as the reference's
-    // running sum); every lane walks the same sequence.
+    T run = T(0);
 #pragma unroll
-    for (int qi = 0; qi < FQ; ++qi) {
-        for (int rr = 0; rr < 32; ++rr) {
-            if (32 * qi + rr >= F) break;
-            T v = __shfl_sync(0xffffffffu, q2[qi], rr);
+    for (int ch = 0; ch < NCH; ++ch) {
+        for (int rr = 0; rr < K; ++rr) {
+            const int r = K * ch + rr;
+            if (r >= F) break;
+            T v = __shfl_sync(0xffffffffu, q2[ch], rr << (5 - LOGK));
             run += v;
-            if (lane == rr) incl[qi] = run;
+            if (lane == (r & 31)) incl[(K * ch) >> 5] = run;
         }
     }
     const T tot = run;

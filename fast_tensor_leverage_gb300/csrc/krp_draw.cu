@@ -68,39 +68,44 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
         double h[XPL];
 #pragma unroll
         for (int q = 0; q < XPL; ++q) h[q] = 1.0;
+#pragma unroll 1
         for (int k = 0; k < p.N; ++k) {
             if ((uint32_t)k == p.j) continue;
-            // eigen-component descent, query h
-            stage_query<RMAX, T>(h, R, xd, xT, lane);
-            qf.setup(xT, pairs, lane);
-            T frac;
-            int64_t c = descend<RMAX>((const T *)p.eig_G + k * eig_stride, p.S, p.eig,
-                                      get_draw(p, (int64_t)k * p.J + i), qf, lane, frac);
-            int64_t u = leaf_index(p.eig, c);
-            const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)u * R;
-            double xs[XPL];
+            // phase 0: eigen-component descent, query h;
+            // phase 1: Gram-tree descent, query h o W[u], leaf scan, h o= U_k[t]
+            double x[XPL];
 #pragma unroll
-            for (int q = 0; q < XPL; ++q) {
-                int col = lane + 32 * q;
-                xs[q] = col < R ? h[q] * Wr[col] : 0.0;
-            }
-            // Gram-tree descent, query h o W[u]
-            __syncwarp();
-            stage_query<RMAX, T>(xs, R, xd, xT, lane);
-            qf.setup(xT, pairs, lane);
-            const DGeom &g = p.gram[k];
-            c = descend<RMAX>((const T *)p.gram_G[k], p.S, g,
-                              get_draw(p, (int64_t)(p.N + k) * p.J + i), qf, lane, frac,
-                              g.F > 1 ? p.U[k] : nullptr, R);
-            int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(p.U[k], R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
-                                : leaf_index(g, c);
-            const double *Ur = p.U[k] + t * R;
+            for (int q = 0; q < XPL; ++q) x[q] = h[q];
+#pragma unroll 1
+            for (int phase = 0; phase < 2; ++phase) {
+                const T *G = phase == 0 ? (const T *)p.eig_G + k * eig_stride : (const T *)p.gram_G[k];
+                const DGeom &g = phase == 0 ? p.eig : p.gram[k];
+                const double *Uk = p.U[k];
+                __syncwarp();
+                stage_query<RMAX, T>(x, R, xd, xT, lane);
+                qf.setup(xT, pairs, lane);
+                T frac;
+                const int64_t c = descend<RMAX>(G, p.S, g, get_draw(p, (int64_t)(phase * p.N + k) * p.J + i),
+                                                qf, lane, frac, (phase == 1 && g.F > 1) ? Uk : nullptr, R);
+                if (phase == 0) {
+                    const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)leaf_index(g, c) * R;
 #pragma unroll
-            for (int q = 0; q < XPL; ++q) {
-                int col = lane + 32 * q;
-                if (col < R) h[q] *= Ur[col];
+                    for (int q = 0; q < XPL; ++q) {
+                        int col = lane + 32 * q;
+                        x[q] = col < R ? h[q] * Wr[col] : 0.0;
+                    }
+                } else {
+                    int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
+                                        : leaf_index(g, c);
+                    const double *Ur = Uk + t * R;
+#pragma unroll
+                    for (int q = 0; q < XPL; ++q) {
+                        int col = lane + 32 * q;
+                        if (col < R) h[q] *= Ur[col];
+                    }
+                    if (lane == 0) p.samples[(int64_t)k * p.J + i] = (uint64_t)t;
+                }
             }
-            if (lane == 0) p.samples[(int64_t)k * p.J + i] = (uint64_t)t;
             __syncwarp();
         }
         if (p.weights) {
