@@ -27,19 +27,19 @@
 #define FTL_DESC_PREFETCH 0        // L2 prefetch of next-level candidates (measured slower)
 #endif
 #ifndef FTL_DESC_XX_SMEM32
-#define FTL_DESC_XX_SMEM32 0       // keep the outer product in shared memory also for R <= 32
+#define FTL_DESC_XX_SMEM32 1       // keep the outer product in shared memory also for R <= 32
 #endif
 #ifndef FTL_DESC_EVAL2
 #define FTL_DESC_EVAL2 1           // root and first-level forms in one round trip
 #endif
 #ifndef FTL_DESC_LEAF_CHUNK
-#define FTL_DESC_LEAF_CHUNK 32     // leaf rows loaded per round trip (8, 16 or 32)
+#define FTL_DESC_LEAF_CHUNK 16     // leaf rows loaded per round trip (8, 16 or 32)
 #endif
 #ifndef FTL_DESC_WARPS32
 #define FTL_DESC_WARPS32 8         // warps per block for R <= 32
 #endif
 #ifndef FTL_DESC_RESIDENT_F32
-#define FTL_DESC_RESIDENT_F32 1024 // threads per SM the FP32 kernels are register-budgeted for
+#define FTL_DESC_RESIDENT_F32 1536 // threads per SM the FP32 kernels are register-budgeted for
 #endif
 #ifndef FTL_DESC_RESIDENT_F64
 #define FTL_DESC_RESIDENT_F64 512
