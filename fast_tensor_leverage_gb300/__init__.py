@@ -6,7 +6,10 @@ cpp_ext/partition_tree.cpp), backed by sm_103a CUDA kernels behind the C ABI
 of include/ftl.h.
 """
 from ._lib import FTLError, PREC
+from .als import ALS, PyLowRank, PySparseTensor, als_prod
 from .partition_tree import PartitionTree
 from .sampler import Sampler
+from .tensors import LowRankTensor, SparseTensor
 
-__all__ = ["FTLError", "PREC", "PartitionTree", "Sampler"]
+__all__ = ["FTLError", "PREC", "PartitionTree", "Sampler", "LowRankTensor", "SparseTensor", "ALS",
+           "PyLowRank", "PySparseTensor", "als_prod"]

@@ -79,6 +79,22 @@ SIGNATURES = {
     "ftl_krp_draw": ([ctypes.POINTER(KRPPlan), _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
     "ftl_krp_sample": ([ctypes.POINTER(KRPPlan), _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
     "ftl_krp_draw_static": ([_INT, _INT, _I64, _INT, _P, _P, _P, _U32, _P, _P, _P, _P, _U64, _U64, _P], _INT),
+    "ftl_fiber_keys": ([_P, _INT, _I64, _I64, _I64, _INT, _P, _INT, _P, _P], _INT),
+    "ftl_sparse_gather": ([_P, _P, _P, _I64, _INT, _INT, _P, _P, _P], _INT),
+    "ftl_dedup_workspace_bytes": ([_I64, _SZP], _INT),
+    "ftl_dedup": ([_P, _I64, _P, ctypes.c_size_t, _P, _P, _P, _P, _P], _INT),
+    "ftl_gram_workspace_bytes": ([_INT, _SZP], _INT),
+    "ftl_weighted_gram": ([_P, _P, _P, _P, _P, _I64, _INT, _P, ctypes.c_size_t, _P, _P], _INT),
+    "ftl_pinv_square": ([_P, _INT, _INT, _P, ctypes.c_double, _P, _P, _P], _INT),
+    "ftl_sparse_mttkrp": ([_P, _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _INT, _P, _I64, _P], _INT),
+    "ftl_solve_rows": ([_P, _P, _I64, _INT, _P, _P], _INT),
+    "ftl_colnorm_workspace_bytes": ([_INT, _SZP], _INT),
+    "ftl_renormalize_columns": ([_P, _I64, _INT, _P, _P, ctypes.c_size_t, _INT, _P], _INT),
+    "ftl_fit_workspace_bytes": ([_SZP], _INT),
+    "ftl_sparse_residual_terms": ([_P, _P, _I64, _INT, _P, _P, _INT, _P, ctypes.c_size_t, _P, _P], _INT),
+    "ftl_sum_squares": ([_P, _I64, _P, ctypes.c_size_t, _P, _P], _INT),
+    "ftl_sparse_exact_mttkrp": ([_P, _P, _I64, _INT, _INT, _P, _INT, _P, _I64, _P], _INT),
+    "ftl_gram_hadamard": ([_P, _INT, _INT, _INT, _P, _P, _P, _P, _P], _INT),
     "ftl_philox_uniforms": ([_P, _I64, _U64, _U64, _P], _INT),
 }
 
@@ -119,6 +135,13 @@ def tree_geometry(n: int, F: int) -> TreeGeom:
 def tree_bytes(n: int, F: int, R: int, prec: int) -> int:
     out = ctypes.c_size_t()
     call("ftl_tree_bytes", n, F, R, prec, ctypes.byref(out))
+    return out.value
+
+
+def ws_bytes(name: str, *args) -> int:
+    """Workspace size query: name is one of dedup / gram / colnorm / fit."""
+    out = ctypes.c_size_t()
+    call(f"ftl_{name}_workspace_bytes", *args, ctypes.byref(out))
     return out.value
 
 

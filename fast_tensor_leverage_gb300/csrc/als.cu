@@ -1,0 +1,698 @@
+// Randomized CP-ALS on a sparse tensor: sampled-fiber dedup, weighted Gram
+// and FP64 pseudo-inverse, sparse MTTKRP through sorted fiber keys, the
+// normal-equation solve, column renormalisation and the fit.
+//
+// Reference semantics (vbharadwaj-bk/fast_tensor_leverage, cpp_ext/):
+//   ALS::execute_ds_als_update        als.hpp:57-220
+//   compute_pinv / compute_pinv_square common.h:228-323
+//   SortIdxLookup ctor / execute_spmm  sort_lookup.hpp:33-132
+//   SortIdxLookup::compute_residual_normsq, ATB_chain_prod_sum
+//                                      sort_lookup.hpp:134-197, common.h:152-226
+//   LowRankTensor::renormalize_columns low_rank_tensor.hpp:203-260
+//   SortIdxLookup::execute_exact_mttkrp sort_lookup.hpp:199-254
+//
+// A fiber key is the mixed-radix number formed by the indices of every mode
+// except j, first mode most significant -- exactly the lexicographic order
+// of the reference's comparators on modes != j.  Sample indices are cast to
+// uint32 first, as the reference does (als.hpp:79, sparse_tensor.hpp:106-109).
+#include <algorithm>
+#include <cstring>
+
+#include "eig.cuh"
+
+namespace ftl {
+
+int num_sms();
+
+struct KeyRadix {
+    int N, j;
+    uint64_t mult[FTL_MAX_MODES];  // place value of mode k (0 for k == j)
+};
+
+static int make_radix(int N, const int64_t *dims, int j, KeyRadix &kr) {
+    FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES, "fiber keys: N=%d outside [1, %d]", N, FTL_MAX_MODES);
+    FTL_CHECK_ARG(dims != nullptr, "fiber keys: dims is NULL");
+    kr.N = N;
+    kr.j = j;
+    // place values from the last mode upwards; the product of the dims of
+    // the modes != j must stay below 2^63
+    unsigned __int128 place = 1;
+    for (int k = N - 1; k >= 0; --k) {
+        FTL_CHECK_ARG(dims[k] >= 1, "fiber keys: dims[%d]=%lld", k, (long long)dims[k]);
+        if (k == j) {
+            kr.mult[k] = 0;
+            continue;
+        }
+        kr.mult[k] = (uint64_t)place;
+        place *= (unsigned __int128)dims[k];
+        if (place > ((unsigned __int128)1 << 63))
+            return fail(FTL_E_UNSUPPORTED,
+                        "fiber keys: the product of the mode sizes other than mode %d exceeds 2^63", j);
+    }
+    for (int k = N; k < FTL_MAX_MODES; ++k) kr.mult[k] = 0;
+    return FTL_OK;
+}
+
+// keys[i] = sum_k (uint32)idx(i, k) * mult[k]; idx element (i, k) at
+// idx[i * si + k * sk] (row-major nnz x N tensors: si = N, sk = 1; the N x J
+// sample layout: si = 1, sk = J).
+template <typename I>
+__global__ void keys_kernel(const I *__restrict__ idx, int64_t n, int64_t si, int64_t sk, KeyRadix kr,
+                            uint64_t *__restrict__ keys) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t key = 0;
+        for (int k = 0; k < kr.N; ++k)
+            if (k != kr.j) key += (uint64_t)(uint32_t)idx[i * si + k * sk] * kr.mult[k];
+        keys[i] = key;
+    }
+}
+
+__global__ void gather_mode_kernel(const int64_t *__restrict__ perm, const uint32_t *__restrict__ idx,
+                                   const double *__restrict__ vals, int64_t nnz, int N, int j,
+                                   uint32_t *__restrict__ idxj, double *__restrict__ vout) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = perm[i];
+        idxj[i] = idx[p * N + j];
+        vout[i] = vals[p];
+    }
+}
+
+static int grid_for(int64_t n, int threads = 256) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, (int64_t)num_sms() * 16));
+}
+
+// ------------------------------------------------------------------ dedup
+
+constexpr uint64_t kEmpty = ~0ull;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    // splitmix64 finaliser
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+__global__ void table_clear_kernel(uint64_t *keys, int32_t *first, int32_t *count, int64_t T) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < T; s += (int64_t)gridDim.x * blockDim.x) {
+        keys[s] = kEmpty;
+        first[s] = INT32_MAX;
+        count[s] = 0;
+    }
+}
+
+// Open addressing with linear probing; at most T probes (T >= 2 J, so a slot
+// is always found).
+__global__ void table_insert_kernel(const uint64_t *__restrict__ skeys, int64_t J, uint64_t *keys,
+                                    int32_t *first, int32_t *count, int64_t T) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < J; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = skeys[i];
+        uint64_t s = mix64(key) & (uint64_t)(T - 1);
+        for (int64_t probe = 0; probe < T; ++probe) {
+            unsigned long long prev = atomicCAS((unsigned long long *)&keys[s], (unsigned long long)kEmpty,
+                                                (unsigned long long)key);
+            if (prev == kEmpty || prev == key) {
+                atomicAdd(&count[s], 1);
+                atomicMin(&first[s], (int32_t)i);
+                break;
+            }
+            s = (s + 1) & (uint64_t)(T - 1);
+        }
+    }
+}
+
+// Deterministic compaction in slot order (one CTA of 1024 threads).
+__global__ void table_compact_kernel(const uint64_t *keys, const int32_t *first, const int32_t *count, int64_t T,
+                                     uint64_t *ukeys, int32_t *urep, int32_t *ucnt, int64_t *num_unique) {
+    __shared__ int warp_tot[32];
+    __shared__ int64_t base_s;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) base_s = 0;
+    __syncthreads();
+    for (int64_t off = 0; off < T; off += blockDim.x) {
+        const int64_t s = off + tid;
+        const int occ = (s < T && keys[s] != kEmpty) ? 1 : 0;
+        unsigned bal = __ballot_sync(0xffffffffu, occ);
+        int pre = __popc(bal & ((1u << lane) - 1));
+        if (lane == 0) warp_tot[warp] = __popc(bal);
+        __syncthreads();
+        int wbase = 0, total = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            if (w < warp) wbase += warp_tot[w];
+            total += warp_tot[w];
+        }
+        if (occ) {
+            int64_t o = base_s + wbase + pre;
+            ukeys[o] = keys[s];
+            urep[o] = first[s];
+            ucnt[o] = count[s];
+        }
+        __syncthreads();
+        if (tid == 0) base_s += total;
+        __syncthreads();
+    }
+    if (tid == 0) *num_unique = base_s;
+}
+
+static int64_t table_size_for(int64_t J) {
+    int64_t T = 1024;
+    while (T < 2 * J) T <<= 1;
+    return T;
+}
+
+// -------------------------------------------------------- weighted Gram
+
+// partial[b][e] = sum over this block's rows u of s_u * h_a h_b, e = packed
+// (a, b); rows u < *n_rows (or n_rows_host), h row = lhs[row(u)], s_u =
+// (w ? w[row(u)] : 1) * (cnt ? cnt[u] : 1).
+__global__ void gram_partial_kernel(const double *__restrict__ lhs, const int32_t *__restrict__ rowidx,
+                                    const double *__restrict__ w, const int32_t *__restrict__ cnt,
+                                    const int64_t *__restrict__ n_rows_dev, int64_t n_rows_host, int R,
+                                    double *__restrict__ partial) {
+    extern __shared__ double hs[];  // 32 rows x R, then P scale slots
+    const int P = packed_size(R);
+    const int64_t n = n_rows_dev ? *n_rows_dev : n_rows_host;
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    double *sc = hs + 32 * R;
+    // entries are covered in passes of 4 per thread
+    for (int e0 = 0; e0 < P; e0 += 4 * blockDim.x) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        int ea[4], eb[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            int e = e0 + threadIdx.x + t * blockDim.x;
+            ea[t] = eb[t] = -1;
+            if (e < P) {
+                int a = 0, rem = e;
+                while (rem >= R - a) {
+                    rem -= R - a;
+                    ++a;
+                }
+                ea[t] = a;
+                eb[t] = a + rem;
+            }
+        }
+        for (int64_t u0 = r0; u0 < r1; u0 += 32) {
+            const int m = (int)min((int64_t)32, r1 - u0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < m * R; e += blockDim.x) {
+                int uu = e / R, col = e - uu * R;
+                int64_t u = u0 + uu;
+                int64_t row = rowidx ? rowidx[u] : u;
+                hs[e] = lhs[row * R + col];
+            }
+            for (int uu = threadIdx.x; uu < m; uu += blockDim.x) {
+                int64_t u = u0 + uu;
+                int64_t row = rowidx ? rowidx[u] : u;
+                sc[uu] = (w ? w[row] : 1.0) * (cnt ? (double)cnt[u] : 1.0);
+            }
+            __syncthreads();
+            for (int uu = 0; uu < m; ++uu) {
+                const double *hr = hs + uu * R;
+                const double su = sc[uu];
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (ea[t] >= 0) acc[t] = fma(su * hr[ea[t]], hr[eb[t]], acc[t]);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (ea[t] >= 0) partial[(int64_t)blockIdx.x * P + e0 + threadIdx.x + t * blockDim.x] = acc[t];
+    }
+}
+
+// out (R x R, full symmetric) = sum of the partials in block order.
+__global__ void gram_reduce_kernel(const double *__restrict__ partial, int nblk, int R, double *__restrict__ out) {
+    const int P = packed_size(R);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < R * R; e += gridDim.x * blockDim.x) {
+        int a = e / R, b = e - a * R;
+        int pe = packed_index(min(a, b), max(a, b), R);
+        double s = 0.0;
+        for (int k = 0; k < nblk; ++k) s += partial[(int64_t)k * P + pe];
+        out[e] = s;
+    }
+}
+
+// --------------------------------------------------------- pseudo-inverse
+
+// compute_pinv_square (common.h:228-269): eigendecomposition of M (upper
+// triangle), keep eigenpair v (ascending rank r) when r >= R - target and
+// lambda > tol, out = sum_kept v v^T / lambda.  target = min(cap, R) with cap
+// read from *rank_cap when given.
+__global__ void pinv_square_kernel(const double *__restrict__ M, int R, int target, const int64_t *rank_cap,
+                                   double tol, double *__restrict__ out, double *vscratch) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int RR = R * R, tid = threadIdx.x, nth = blockDim.x;
+    double *A = (double *)smem_raw;
+    double *V = vscratch ? vscratch : A + RR;
+    double *cs = A + (vscratch ? 1 : 2) * RR;
+    int *pq = (int *)(cs + R + 2);
+    int *order = pq + R + 2;
+    int *flag = order + R;
+    for (int e = tid; e < RR; e += nth) {
+        int a = e / R, b = e - a * R;
+        A[e] = a <= b ? M[e] : M[b * R + a];
+    }
+    __syncthreads();
+    jacobi_eigen<double>(A, V, R, cs, pq, flag);
+    sort_ascending<double>(A, R, order);
+    int tr = target;
+    if (rank_cap) tr = (int)min((int64_t)R, *rank_cap);
+    for (int e = tid; e < RR; e += nth) {
+        int a = e / R, b = e - a * R;
+        double s = 0.0;
+        for (int r = 0; r < R; ++r) {
+            const int v = order[r];
+            const double lam = A[v * R + v];
+            if (r >= R - tr && lam > tol) s += (V[a * R + v] / sqrt(lam)) * (V[b * R + v] / sqrt(lam));
+        }
+        out[e] = s;
+    }
+}
+
+// ------------------------------------------------------------- MTTKRP
+
+// One warp per query: lower_bound of the query's fiber key in the sorted
+// keys, then out[idx_j, :] += value * scale * lhs[row, :] for every nonzero
+// of the fiber (SortIdxLookup::execute_spmm, sort_lookup.hpp:69-132).
+__global__ void mttkrp_kernel(const uint64_t *__restrict__ skeys, const uint32_t *__restrict__ sidx,
+                              const double *__restrict__ svals, int64_t nnz, const uint64_t *__restrict__ qkeys,
+                              const int32_t *__restrict__ qrow, const double *__restrict__ w,
+                              const int32_t *__restrict__ cnt, const int64_t *__restrict__ nq_dev, int64_t nq_host,
+                              const double *__restrict__ lhs, int R, double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nq = nq_dev ? *nq_dev : nq_host;
+    for (int64_t q = warp; q < nq; q += nwarps) {
+        const uint64_t key = qkeys[q];
+        int64_t lo = 0, hi = nnz;
+        while (lo < hi) {
+            int64_t mid = lo + (hi - lo) / 2;
+            if (skeys[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo >= nnz || skeys[lo] != key) continue;
+        const int64_t row = qrow ? qrow[q] : q;
+        const double scale = (w ? w[row] : 1.0) * (cnt ? (double)cnt[q] : 1.0);
+        for (int64_t z = lo; z < nnz && skeys[z] == key; ++z) {
+            const double v = svals[z] * scale;
+            double *o = out + (int64_t)sidx[z] * R;
+            for (int col = lane; col < R; col += 32) atomicAdd(o + col, v * lhs[row * R + col]);
+        }
+    }
+}
+
+// ------------------------------------------------------ solve / renorm
+
+// U = B pinv (pinv R x R symmetric) row by row; an all-zero row of B (a row
+// no sampled fiber touched) is written as zeros without arithmetic.
+__global__ void solve_rows_kernel(const double *__restrict__ B, const double *__restrict__ pinv, int64_t I, int R,
+                                  double *__restrict__ U) {
+    extern __shared__ double sm[];
+    double *ps = sm;               // R x R
+    double *bs = sm + R * R;       // blockDim.x rows x R (row-major)
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) ps[e] = pinv[e];
+    for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x; r0 < I; r0 += (int64_t)gridDim.x * blockDim.x) {
+        const int m = (int)min((int64_t)blockDim.x, I - r0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < m * R; e += blockDim.x) bs[e] = B[r0 * R + e];
+        __syncthreads();
+        if (threadIdx.x < m) {
+            const double *b = bs + threadIdx.x * R;
+            bool any = false;
+            for (int c = 0; c < R; ++c) any |= (b[c] != 0.0);
+            double *o = bs + threadIdx.x * R;
+            if (any) {
+                double tmp[FTL_MAX_RANK];
+                for (int c = 0; c < R; ++c) tmp[c] = b[c];
+                for (int c = 0; c < R; ++c) {
+                    double s = 0.0;
+                    for (int k = 0; k < R; ++k) s = fma(tmp[k], ps[k * R + c], s);
+                    o[c] = s;
+                }
+            }
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < m * R; e += blockDim.x) U[r0 * R + e] = bs[e];
+    }
+}
+
+__global__ void colsq_partial_kernel(const double *__restrict__ U, int64_t I, int R, double *__restrict__ partial) {
+    // thread t accumulates column (t % R) over rows t / R, t / R + stride ...
+    const int tid = threadIdx.x;
+    const int rows_per_pass = blockDim.x / R;
+    double acc = 0.0;
+    const int col = tid % R, r_in = tid / R;
+    if (r_in < rows_per_pass) {
+        for (int64_t r = (int64_t)blockIdx.x * rows_per_pass + r_in; r < I; r += (int64_t)gridDim.x * rows_per_pass) {
+            double x = U[r * R + col];
+            acc = fma(x, x, acc);
+        }
+    }
+    __shared__ double red[1024];
+    red[tid] = (r_in < rows_per_pass) ? acc : 0.0;
+    __syncthreads();
+    if (tid < R) {
+        double s = 0.0;
+        for (int k = 0; k < rows_per_pass; ++k) s += red[k * R + tid];
+        partial[(int64_t)blockIdx.x * R + tid] = s;
+    }
+}
+
+// norms: sqrt of the column sums, <= 1e-7 -> 1 (low_rank_tensor.hpp:229-238)
+__global__ void colnorm_finish_kernel(const double *__restrict__ partial, int nblk, int R, double *__restrict__ norms) {
+    for (int c = threadIdx.x; c < R; c += blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < nblk; ++k) s += partial[(int64_t)k * R + c];
+        double n = sqrt(s);
+        norms[c] = n <= 1e-7 ? 1.0 : n;
+    }
+}
+
+__global__ void colscale_kernel(double *__restrict__ U, int64_t I, int R, const double *__restrict__ norms) {
+    const int64_t total = I * R;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+        U[e] = U[e] / norms[e % R];
+}
+
+// ------------------------------------------------------------ fit terms
+
+struct FactorPtrs {
+    const double *U[FTL_MAX_MODES];
+};
+
+// partial[b] = sum over this block's nonzeros of v^2 - 2 v model(idx), model
+// = sum_r sigma_r prod_k U_k[idx_k, r] (sort_lookup.hpp:183-191); one warp
+// per nonzero, lanes over r.
+__global__ void residual_partial_kernel(const uint32_t *__restrict__ idx, const double *__restrict__ vals,
+                                        int64_t nnz, int N, FactorPtrs fp, const double *__restrict__ sigma,
+                                        int R, double *__restrict__ partial) {
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double acc = 0.0;
+    for (int64_t z = gw; z < nnz; z += nw) {
+        double m = 0.0;
+        for (int r = lane; r < R; r += 32) {
+            double p = sigma[r];
+            for (int k = 0; k < N; ++k) p *= fp.U[k][(int64_t)idx[z * N + k] * R + r];
+            m += p;
+        }
+        m = warp_sum(m);
+        const double v = vals[z];
+        if (lane == 0) acc += v * v - 2.0 * m * v;
+    }
+    if (lane == 0) red[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        partial[blockIdx.x] = s;
+    }
+}
+
+__global__ void sum_kernel(const double *__restrict__ partial, int n, double *__restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < n; ++k) s += partial[k];
+        *out = s;
+    }
+}
+
+__global__ void sumsq_partial_kernel(const double *__restrict__ v, int64_t n, double *__restrict__ partial) {
+    __shared__ double red[1024];
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc = fma(v[i], v[i], acc);
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) s += red[t];
+        partial[blockIdx.x] = s;
+    }
+}
+
+// Exact MTTKRP (sort_lookup.hpp:199-254): out[idx_j] += v * prod_{k != j} U_k[idx_k]
+__global__ void exact_mttkrp_kernel(const uint32_t *__restrict__ idx, const double *__restrict__ vals, int64_t nnz,
+                                    int N, int j, FactorPtrs fp, int R, double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t z = gw; z < nnz; z += nw) {
+        const double v = vals[z];
+        double *o = out + (int64_t)idx[z * N + j] * R;
+        for (int r = lane; r < R; r += 32) {
+            double p = 1.0;
+            for (int k = 0; k < N; ++k)
+                if (k != j) p *= fp.U[k][(int64_t)idx[z * N + k] * R + r];
+            atomicAdd(o + r, v * p);
+        }
+    }
+}
+
+struct GramPtrs {
+    const double *G[FTL_MAX_MODES];
+};
+
+// M = (sa sb^T) o prod_{k != exclude} G_k (ATB_chain_prod, common.h:152-213);
+// optionally out_sum = sum of M's entries (ATB_chain_prod_sum, :215-226).
+__global__ void gram_hadamard_kernel(GramPtrs gp, int N, int R, int exclude, const double *__restrict__ sa,
+                                     const double *__restrict__ sb, double *__restrict__ out_mat,
+                                     double *__restrict__ out_sum) {
+    __shared__ double red[1024];
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+        int a = e / R, b = e - a * R;
+        double m = (sa ? sa[a] : 1.0) * (sb ? sb[b] : 1.0);
+        for (int k = 0; k < N; ++k)
+            if (k != exclude) m *= gp.G[k][e];
+        if (out_mat) out_mat[e] = m;
+        acc += m;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0 && out_sum) {
+        double s = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t) s += red[t];
+        *out_sum = s;
+    }
+}
+
+}  // namespace ftl
+
+using namespace ftl;
+
+// ============================================================== C ABI
+
+extern "C" int ftl_gram_hadamard(const double *const *grams_dev, int N, int R, int exclude, const double *sigma_a,
+                                 const double *sigma_b, double *out_mat, double *out_sum, void *stream) {
+    FTL_CHECK_ARG(grams_dev && (out_mat || out_sum), "ftl_gram_hadamard: null pointer");
+    FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && R >= 1 && R <= FTL_MAX_RANK, "ftl_gram_hadamard: bad shape");
+    GramPtrs gp;
+    for (int k = 0; k < FTL_MAX_MODES; ++k) gp.G[k] = k < N ? grams_dev[k] : nullptr;
+    gram_hadamard_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(gp, N, R, exclude, sigma_a, sigma_b, out_mat, out_sum);
+    return check_launch("gram_hadamard_kernel");
+}
+
+extern "C" int ftl_fiber_keys(const void *idx, int idx_is_u64, int64_t n, int64_t stride_item, int64_t stride_mode,
+                              int N, const int64_t *dims, int j, uint64_t *keys_out, void *stream) {
+    FTL_CHECK_ARG(idx && keys_out, "ftl_fiber_keys: null pointer");
+    FTL_CHECK_ARG(n >= 0, "ftl_fiber_keys: n=%lld", (long long)n);
+    KeyRadix kr;
+    int rc = make_radix(N, dims, j, kr);
+    if (rc) return rc;
+    if (n == 0) return FTL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (idx_is_u64)
+        keys_kernel<uint64_t><<<grid_for(n), 256, 0, st>>>((const uint64_t *)idx, n, stride_item, stride_mode, kr, keys_out);
+    else
+        keys_kernel<uint32_t><<<grid_for(n), 256, 0, st>>>((const uint32_t *)idx, n, stride_item, stride_mode, kr, keys_out);
+    return check_launch("keys_kernel");
+}
+
+extern "C" int ftl_sparse_gather(const int64_t *perm, const uint32_t *idx, const double *vals, int64_t nnz, int N,
+                                 int j, uint32_t *idxj_out, double *vals_out, void *stream) {
+    FTL_CHECK_ARG(perm && idx && vals && idxj_out && vals_out, "ftl_sparse_gather: null pointer");
+    FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && j >= 0 && j < N, "ftl_sparse_gather: bad N=%d j=%d", N, j);
+    if (nnz == 0) return FTL_OK;
+    gather_mode_kernel<<<grid_for(nnz), 256, 0, (cudaStream_t)stream>>>(perm, idx, vals, nnz, N, j, idxj_out, vals_out);
+    return check_launch("gather_mode_kernel");
+}
+
+extern "C" int ftl_dedup_workspace_bytes(int64_t J, size_t *out) {
+    FTL_CHECK_ARG(out && J >= 1 && J <= INT32_MAX / 2, "ftl_dedup_workspace_bytes: bad J=%lld", (long long)J);
+    *out = (size_t)table_size_for(J) * (sizeof(uint64_t) + 2 * sizeof(int32_t));
+    return FTL_OK;
+}
+
+extern "C" int ftl_dedup(const uint64_t *keys, int64_t J, void *workspace, size_t ws_bytes, uint64_t *ukeys,
+                         int32_t *urep, int32_t *ucnt, int64_t *num_unique, void *stream) {
+    FTL_CHECK_ARG(keys && workspace && ukeys && urep && ucnt && num_unique, "ftl_dedup: null pointer");
+    size_t need = 0;
+    int rc = ftl_dedup_workspace_bytes(J, &need);
+    if (rc) return rc;
+    FTL_CHECK_ARG(ws_bytes >= need, "ftl_dedup: workspace %zu < %zu bytes", ws_bytes, need);
+    const int64_t T = table_size_for(J);
+    uint64_t *tk = (uint64_t *)workspace;
+    int32_t *tf = (int32_t *)(tk + T);
+    int32_t *tc = tf + T;
+    cudaStream_t st = (cudaStream_t)stream;
+    table_clear_kernel<<<grid_for(T), 256, 0, st>>>(tk, tf, tc, T);
+    table_insert_kernel<<<grid_for(J), 256, 0, st>>>(keys, J, tk, tf, tc, T);
+    table_compact_kernel<<<1, 1024, 0, st>>>(tk, tf, tc, T, ukeys, urep, ucnt, num_unique);
+    return check_launch("dedup kernels");
+}
+
+extern "C" int ftl_gram_workspace_bytes(int R, size_t *out) {
+    FTL_CHECK_ARG(out && R >= 1 && R <= FTL_MAX_RANK, "ftl_gram_workspace_bytes: bad R=%d", R);
+    *out = (size_t)num_sms() * packed_size(R) * sizeof(double);
+    return FTL_OK;
+}
+
+extern "C" int ftl_weighted_gram(const double *lhs, const int32_t *rowidx, const double *w, const int32_t *cnt,
+                                 const int64_t *n_rows_dev, int64_t n_rows, int R, void *workspace, size_t ws_bytes,
+                                 double *gram_out, void *stream) {
+    FTL_CHECK_ARG(lhs && workspace && gram_out, "ftl_weighted_gram: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK, "ftl_weighted_gram: bad R=%d", R);
+    size_t need = 0;
+    ftl_gram_workspace_bytes(R, &need);
+    FTL_CHECK_ARG(ws_bytes >= need, "ftl_weighted_gram: workspace %zu < %zu bytes", ws_bytes, need);
+    const int nblk = num_sms();
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t smem = (size_t)(32 * R + 32) * sizeof(double);
+    gram_partial_kernel<<<nblk, 256, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, (double *)workspace);
+    gram_reduce_kernel<<<std::max(1, (R * R + 255) / 256), 256, 0, st>>>((const double *)workspace, nblk, R, gram_out);
+    return check_launch("weighted gram kernels");
+}
+
+extern "C" int ftl_pinv_square(const double *M, int R, int target_rank, const int64_t *rank_cap_dev, double tol,
+                               double *out, double *vscratch, void *stream) {
+    FTL_CHECK_ARG(M && out, "ftl_pinv_square: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK, "ftl_pinv_square: bad R=%d", R);
+    const bool vglob = (size_t)(2 * R * R + R + 2) * sizeof(double) > 200 * 1024;
+    FTL_CHECK_ARG(!vglob || vscratch, "ftl_pinv_square: R=%d needs an R*R FP64 scratch buffer", R);
+    const size_t smem = (size_t)((vglob ? 1 : 2) * R * R + R + 2) * sizeof(double) + (2 * R + 4) * sizeof(int) + 16;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(pinv_square_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    pinv_square_kernel<<<1, 512, smem, (cudaStream_t)stream>>>(M, R, target_rank, rank_cap_dev, tol, out,
+                                                                vglob ? vscratch : nullptr);
+    return check_launch("pinv_square_kernel");
+}
+
+extern "C" int ftl_sparse_mttkrp(const uint64_t *sorted_keys, const uint32_t *sorted_idxj, const double *sorted_vals,
+                                 int64_t nnz, const uint64_t *query_keys, const int32_t *query_row, const double *w,
+                                 const int32_t *cnt, const int64_t *num_queries_dev, int64_t num_queries,
+                                 const double *lhs, int R, double *out, int64_t I_j, void *stream) {
+    FTL_CHECK_ARG(sorted_keys && sorted_idxj && sorted_vals && query_keys && lhs && out,
+                  "ftl_sparse_mttkrp: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1, "ftl_sparse_mttkrp: bad R=%d or I_j", R);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t err = cudaMemsetAsync(out, 0, (size_t)I_j * R * sizeof(double), st);
+    if (err != cudaSuccess) return fail(FTL_E_CUDA, "ftl_sparse_mttkrp: memset: %s", cudaGetErrorString(err));
+    if (nnz == 0) return FTL_OK;
+    const int64_t nq = std::max<int64_t>(num_queries, 1);
+    int blocks = (int)std::min<int64_t>((nq * 32 + 255) / 256, (int64_t)num_sms() * 16);
+    mttkrp_kernel<<<std::max(blocks, 1), 256, 0, st>>>(sorted_keys, sorted_idxj, sorted_vals, nnz, query_keys,
+                                                        query_row, w, cnt, num_queries_dev, num_queries, lhs, R, out);
+    return check_launch("mttkrp_kernel");
+}
+
+extern "C" int ftl_solve_rows(const double *B, const double *pinv, int64_t I, int R, double *U, void *stream) {
+    FTL_CHECK_ARG(B && pinv && U, "ftl_solve_rows: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I >= 1, "ftl_solve_rows: bad shape");
+    const int threads = 128;
+    const size_t smem = (size_t)(R * R + threads * R) * sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(solve_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    FTL_CHECK_ARG(smem <= 227 * 1024, "ftl_solve_rows: R=%d too large", R);
+    int blocks = (int)std::min<int64_t>((I + threads - 1) / threads, (int64_t)num_sms() * 8);
+    solve_rows_kernel<<<blocks, threads, smem, (cudaStream_t)stream>>>(B, pinv, I, R, U);
+    return check_launch("solve_rows_kernel");
+}
+
+extern "C" int ftl_colnorm_workspace_bytes(int R, size_t *out) {
+    FTL_CHECK_ARG(out && R >= 1 && R <= FTL_MAX_RANK, "ftl_colnorm_workspace_bytes: bad R");
+    *out = (size_t)num_sms() * 4 * R * sizeof(double);
+    return FTL_OK;
+}
+
+extern "C" int ftl_renormalize_columns(double *U, int64_t I, int R, double *norms_out, void *workspace,
+                                       size_t ws_bytes, int apply, void *stream) {
+    FTL_CHECK_ARG(U && norms_out && workspace, "ftl_renormalize_columns: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I >= 1, "ftl_renormalize_columns: bad shape");
+    size_t need = 0;
+    ftl_colnorm_workspace_bytes(R, &need);
+    FTL_CHECK_ARG(ws_bytes >= need, "ftl_renormalize_columns: workspace too small");
+    const int nblk = num_sms() * 4;
+    const int threads = std::max(R, 1024 / R * R);
+    cudaStream_t st = (cudaStream_t)stream;
+    colsq_partial_kernel<<<nblk, threads, 0, st>>>(U, I, R, (double *)workspace);
+    colnorm_finish_kernel<<<1, 128, 0, st>>>((const double *)workspace, nblk, R, norms_out);
+    if (apply) colscale_kernel<<<grid_for(I * R), 256, 0, st>>>(U, I, R, norms_out);
+    return check_launch("renormalize kernels");
+}
+
+extern "C" int ftl_fit_workspace_bytes(size_t *out) {
+    FTL_CHECK_ARG(out, "ftl_fit_workspace_bytes: null");
+    *out = (size_t)num_sms() * 16 * sizeof(double);
+    return FTL_OK;
+}
+
+extern "C" int ftl_sparse_residual_terms(const uint32_t *idx, const double *vals, int64_t nnz, int N,
+                                         const double *const *U_dev, const double *sigma, int R, void *workspace,
+                                         size_t ws_bytes, double *out, void *stream) {
+    FTL_CHECK_ARG(idx && vals && U_dev && sigma && workspace && out, "ftl_sparse_residual_terms: null pointer");
+    FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && R >= 1 && R <= FTL_MAX_RANK, "ftl_sparse_residual_terms: bad shape");
+    size_t need = 0;
+    ftl_fit_workspace_bytes(&need);
+    FTL_CHECK_ARG(ws_bytes >= need, "ftl_sparse_residual_terms: workspace too small");
+    FactorPtrs fp;
+    for (int k = 0; k < FTL_MAX_MODES; ++k) fp.U[k] = k < N ? U_dev[k] : nullptr;
+    const int nblk = num_sms() * 16;
+    cudaStream_t st = (cudaStream_t)stream;
+    residual_partial_kernel<<<nblk, 256, 0, st>>>(idx, vals, nnz, N, fp, sigma, R, (double *)workspace);
+    sum_kernel<<<1, 32, 0, st>>>((const double *)workspace, nblk, out);
+    return check_launch("residual kernels");
+}
+
+extern "C" int ftl_sum_squares(const double *v, int64_t n, void *workspace, size_t ws_bytes, double *out,
+                               void *stream) {
+    FTL_CHECK_ARG(v && workspace && out, "ftl_sum_squares: null pointer");
+    size_t need = 0;
+    ftl_fit_workspace_bytes(&need);
+    FTL_CHECK_ARG(ws_bytes >= need, "ftl_sum_squares: workspace too small");
+    const int nblk = num_sms() * 16;
+    cudaStream_t st = (cudaStream_t)stream;
+    sumsq_partial_kernel<<<nblk, 256, 0, st>>>(v, n, (double *)workspace);
+    sum_kernel<<<1, 32, 0, st>>>((const double *)workspace, nblk, out);
+    return check_launch("sum of squares kernels");
+}
+
+extern "C" int ftl_sparse_exact_mttkrp(const uint32_t *idx, const double *vals, int64_t nnz, int N, int j,
+                                       const double *const *U_dev, int R, double *out, int64_t I_j, void *stream) {
+    FTL_CHECK_ARG(idx && vals && U_dev && out, "ftl_sparse_exact_mttkrp: null pointer");
+    FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && j >= 0 && j < N && R >= 1 && R <= FTL_MAX_RANK,
+                  "ftl_sparse_exact_mttkrp: bad shape");
+    FactorPtrs fp;
+    for (int k = 0; k < FTL_MAX_MODES; ++k) fp.U[k] = k < N ? U_dev[k] : nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t err = cudaMemsetAsync(out, 0, (size_t)I_j * R * sizeof(double), st);
+    if (err != cudaSuccess) return fail(FTL_E_CUDA, "ftl_sparse_exact_mttkrp: memset: %s", cudaGetErrorString(err));
+    if (nnz == 0) return FTL_OK;
+    exact_mttkrp_kernel<<<num_sms() * 16, 256, 0, st>>>(idx, vals, nnz, N, j, fp, R, out);
+    return check_launch("exact_mttkrp_kernel");
+}

@@ -1,0 +1,258 @@
+"""LowRankTensor and SparseTensor: drop-ins for the reference's tensor
+classes on the CP-ALS path (cpp_ext/low_rank_tensor.hpp:13-303,
+cpp_ext/sparse_tensor.hpp:25-213, bound in cpp_ext/als_module.cpp:85-107),
+with factors and nonzeros resident on the GPU."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _device as D
+from . import _lib
+
+
+def _ptrs(tensors) -> ctypes.Array:
+    arr = (ctypes.c_void_p * len(tensors))()
+    for k, t in enumerate(tensors):
+        arr[k] = t.data_ptr()
+    return arr
+
+
+class _Workspace:
+    """Device scratch buffers reused across calls, keyed by name."""
+
+    def __init__(self, device):
+        self.device = device
+        self._bufs = {}
+
+    def get(self, name: str, nbytes: int) -> torch.Tensor:
+        b = self._bufs.get(name)
+        if b is None or b.numel() < nbytes:
+            b = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=self.device)
+            self._bufs[name] = b
+        return b
+
+
+def factor_gram(U_dev: torch.Tensor, ws: _Workspace, stream: int, out: torch.Tensor | None = None) -> torch.Tensor:
+    """FP64 U^T U (R x R) on the device."""
+    I, R = U_dev.shape
+    if out is None:
+        out = torch.empty((R, R), dtype=torch.float64, device=U_dev.device)
+    gb = _lib.ws_bytes("gram", R)
+    w = ws.get("gram", gb)
+    _lib.call("ftl_weighted_gram", U_dev.data_ptr(), None, None, None, None, I, R, w.data_ptr(), gb,
+              out.data_ptr(), stream)
+    return out
+
+
+class LowRankTensor:
+    """CP model sum_r sigma_r u_r^(1) o ... o u_r^(N).
+
+    LowRankTensor(R, U_list) or LowRankTensor(R, max_rhs_rows, U_list), as in
+    the reference.  U_list holds float64 (I_k, R) C-contiguous numpy arrays,
+    kept by reference; ALS updates are mirrored back into them (set
+    `sync_host=False` to keep the factors on the device only and call
+    `sync_host_copies()` when the host arrays are needed)."""
+
+    def __init__(self, R, *args, device=None, sync_host: bool = True):
+        if len(args) == 1:
+            U_list, self.max_rhs_rows, self.is_static = args[0], None, False
+        elif len(args) == 2:
+            self.max_rhs_rows, U_list = int(args[0]), args[1]
+            self.is_static = True
+        else:
+            raise TypeError("LowRankTensor(R, U_list) or LowRankTensor(R, max_rhs_rows, U_list)")
+        self.R = int(R)
+        self.U = list(U_list)
+        self.N = len(self.U)
+        if not (1 <= self.N <= _lib.MAX_MODES) or not (1 <= self.R <= _lib.MAX_RANK):
+            raise ValueError(f"bad N={self.N} or R={self.R}")
+        for k, u in enumerate(self.U):
+            D.require_numpy_out(u, np.float64, f"U[{k}]")
+            if u.ndim != 2 or u.shape[1] != self.R:
+                raise ValueError(f"U[{k}] must be (I_k, {self.R}), got {u.shape}")
+        self.dims = [int(u.shape[0]) for u in self.U]
+        self.device = D.cuda_device(device)
+        self.U_dev = [torch.from_numpy(u).to(self.device) for u in self.U]
+        self.sigma_dev = torch.ones(self.R, dtype=torch.float64, device=self.device)
+        self.sync_host = sync_host
+        self._ws = _Workspace(self.device)
+        self._normsq = None
+        if self.is_static:
+            self._normsq = self._chain_sum_self()
+
+    # ---------------------------------------------------------- plumbing
+    def _stream(self) -> int:
+        return D.stream_ptr(self.device)
+
+    def upload(self, k: int | None = None) -> None:
+        """Copy host factor(s) to the device (after editing the numpy arrays)."""
+        for i in range(self.N) if k is None else [k]:
+            self.U_dev[i].copy_(torch.from_numpy(self.U[i]))
+
+    def sync_host_copies(self, k: int | None = None) -> None:
+        for i in range(self.N) if k is None else [k]:
+            self.U[i][...] = self.U_dev[i].cpu().numpy()
+
+    @property
+    def sigma(self) -> np.ndarray:
+        return self.sigma_dev.cpu().numpy()
+
+    # ------------------------------------------------------------ sigma
+    def get_sigma(self, out, j: int = -1) -> None:
+        o = D.require_numpy_out(out, np.float64, "sigma_out", min_size=self.R)
+        o.reshape(-1)[: self.R] = self.sigma
+
+    def set_sigma(self, sigma_in) -> None:
+        s = np.ascontiguousarray(np.asarray(sigma_in, dtype=np.float64).reshape(-1)[: self.R])
+        self.sigma_dev.copy_(torch.from_numpy(s))
+
+    # ------------------------------------------------------ renormalise
+    def renormalize_columns(self, j: int) -> None:
+        """Divide the columns of factor j (j = -1: every factor) by their
+        norms (norms <= 1e-7 count as 1); sigma <- the norms of factor j, or
+        the product over all factors for j = -1
+        (low_rank_tensor.hpp:203-260)."""
+        st = self._stream()
+        nb = _lib.ws_bytes("colnorm", self.R)
+        w = self._ws.get("colnorm", nb)
+        modes = range(self.N) if j == -1 else [j]
+        norms = torch.empty((self.N, self.R), dtype=torch.float64, device=self.device)
+        for i in modes:
+            _lib.call("ftl_renormalize_columns", self.U_dev[i].data_ptr(), self.dims[i], self.R,
+                      norms[i].data_ptr(), w.data_ptr(), nb, 1, st)
+        if j == -1:
+            self.sigma_dev.copy_(torch.prod(norms, dim=0))
+        else:
+            self.sigma_dev.copy_(norms[j])
+        self._normsq = None if not self.is_static else self._normsq
+        if self.sync_host:
+            for i in modes:
+                self.sync_host_copies(i)
+
+    # ------------------------------------------------------------ norms
+    def grams(self) -> list[torch.Tensor]:
+        st = self._stream()
+        return [factor_gram(u, self._ws, st) for u in self.U_dev]
+
+    def _chain_sum_self(self) -> float:
+        G = self.grams()
+        out = torch.empty(1, dtype=torch.float64, device=self.device)
+        _lib.call("ftl_gram_hadamard", _ptrs(G), self.N, self.R, -1, self.sigma_dev.data_ptr(),
+                  self.sigma_dev.data_ptr(), None, out.data_ptr(), self._stream())
+        return float(out.item())
+
+    def get_normsq(self) -> float:
+        """||model||^2 = sum_rs sigma_r sigma_s prod_k (U_k^T U_k)_rs
+        (low_rank_tensor.hpp:70-76)."""
+        if not self.is_static or self._normsq is None:
+            return self._chain_sum_self()
+        return self._normsq
+
+
+class SparseTensor:
+    """COO tensor with one sorted fiber lookup per mode
+    (SparseTensor, sparse_tensor.hpp:46-77; SortIdxLookup ctor,
+    sort_lookup.hpp:33-60).  idx: (nnz, N) uint32, vals: (nnz,) float64."""
+
+    def __init__(self, idx, vals, method: str = "sort", *, dims=None, device=None):
+        if method != "sort":
+            raise ValueError(f"Unknown lookup method {method!r} (only 'sort' is implemented)")
+        idx = np.asarray(idx)
+        if idx.ndim != 2 or idx.dtype != np.uint32:
+            raise TypeError("idx must be a (nnz, N) uint32 array")
+        vals = np.ascontiguousarray(np.asarray(vals, dtype=np.float64).reshape(-1))
+        if vals.shape[0] != idx.shape[0]:
+            raise ValueError("idx and vals disagree on nnz")
+        self.nnz, self.N = int(idx.shape[0]), int(idx.shape[1])
+        self.device = D.cuda_device(device)
+        dev = self.device
+        st = D.stream_ptr(dev)
+        self.idx_dev = torch.from_numpy(np.ascontiguousarray(idx).view(np.int32)).to(dev)
+        self.vals_dev = torch.from_numpy(vals).to(dev)
+        if dims is None:
+            dims = (idx.max(axis=0).astype(np.int64) + 1) if self.nnz else np.ones(self.N, np.int64)
+        self.dims = [int(d) for d in dims]
+        dims_c = (ctypes.c_int64 * self.N)(*self.dims)
+        self._ws = _Workspace(dev)
+        self.lookups = []
+        for j in range(self.N):
+            keys = torch.empty(self.nnz, dtype=torch.int64, device=dev)
+            _lib.call("ftl_fiber_keys", self.idx_dev.data_ptr(), 0, self.nnz, self.N, 1, self.N, dims_c, j,
+                      keys.data_ptr(), st)
+            # one-off construction sort of the fiber keys (keys < 2^63, so the
+            # signed order is the unsigned order)
+            skeys, perm = torch.sort(keys)
+            idxj = torch.empty(self.nnz, dtype=torch.int32, device=dev)
+            vj = torch.empty(self.nnz, dtype=torch.float64, device=dev)
+            _lib.call("ftl_sparse_gather", perm.data_ptr(), self.idx_dev.data_ptr(), self.vals_dev.data_ptr(),
+                      self.nnz, self.N, j, idxj.data_ptr(), vj.data_ptr(), st)
+            del perm, keys
+            self.lookups.append((skeys, idxj, vj))
+        nb = _lib.ws_bytes("fit")
+        out = torch.empty(1, dtype=torch.float64, device=dev)
+        _lib.call("ftl_sum_squares", self.vals_dev.data_ptr(), self.nnz, self._ws.get("fit", nb).data_ptr(), nb,
+                  out.data_ptr(), st)
+        self.normsq = float(out.item())
+        self._dims_c = dims_c
+
+    def get_normsq(self) -> float:
+        return self.normsq
+
+    def _factor_dev(self, U_list, R):
+        out = []
+        for k, u in enumerate(U_list):
+            if isinstance(u, torch.Tensor) and u.is_cuda:
+                out.append(u.to(torch.float64).contiguous())
+            else:
+                out.append(torch.from_numpy(D.as_factor(u, R, f"U[{k}]")).to(self.device))
+        return out
+
+    def compute_residual_normsq(self, sigma, U_list) -> float:
+        """||X - [[sigma; U]]||^2 = sum_nnz (v^2 - 2 v model) + ||model||^2
+        (sparse_tensor.hpp:117-119, sort_lookup.hpp:134-197).  U_list items
+        may be numpy arrays or CUDA tensors (a LowRankTensor's U_dev)."""
+        st = D.stream_ptr(self.device)
+        if isinstance(sigma, torch.Tensor):
+            sig = sigma.to(self.device, torch.float64).contiguous()
+        else:
+            sig = torch.from_numpy(np.ascontiguousarray(np.asarray(sigma, dtype=np.float64))).to(self.device)
+        R = int(sig.numel())
+        Ud = self._factor_dev(U_list, R)
+        nb = _lib.ws_bytes("fit")
+        terms = torch.empty(2, dtype=torch.float64, device=self.device)
+        _lib.call("ftl_sparse_residual_terms", self.idx_dev.data_ptr(), self.vals_dev.data_ptr(), self.nnz, self.N,
+                  _ptrs(Ud), sig.data_ptr(), R, self._ws.get("fit", nb).data_ptr(), nb, terms[0:1].data_ptr(), st)
+        G = [factor_gram(u, self._ws, st) for u in Ud]
+        _lib.call("ftl_gram_hadamard", _ptrs(G), self.N, R, -1, sig.data_ptr(), sig.data_ptr(), None,
+                  terms[1:2].data_ptr(), st)
+        t = terms.cpu().numpy()
+        return float(t[0] + t[1])
+
+    def execute_downsampled_mttkrp_py(self, samples, lhs, j: int, result) -> None:
+        """result (I_j x R) = sum over the rows i of samples (J x N uint64) of
+        the fiber of samples[i] (modes != j) times lhs[i]
+        (sparse_tensor.hpp:95-115)."""
+        s = np.ascontiguousarray(np.asarray(samples, dtype=np.uint64))
+        J, N = s.shape
+        if N != self.N:
+            raise ValueError(f"samples has {N} modes, tensor {self.N}")
+        lhs_np = np.ascontiguousarray(np.asarray(lhs, dtype=np.float64))
+        R = lhs_np.shape[1]
+        out = D.require_numpy_out(result, np.float64, "result")
+        if out.shape != (self.dims[j], R) and out.shape[0] < self.dims[j]:
+            raise ValueError(f"result must be ({self.dims[j]}, {R})")
+        dev = self.device
+        st = D.stream_ptr(dev)
+        s_d = torch.from_numpy(s.view(np.int64)).to(dev)
+        keys = torch.empty(J, dtype=torch.int64, device=dev)
+        _lib.call("ftl_fiber_keys", s_d.data_ptr(), 1, J, N, 1, N, self._dims_c, j, keys.data_ptr(), st)
+        lhs_d = torch.from_numpy(lhs_np).to(dev)
+        I_j = out.shape[0]
+        o = torch.empty((I_j, R), dtype=torch.float64, device=dev)
+        skeys, idxj, vj = self.lookups[j]
+        _lib.call("ftl_sparse_mttkrp", skeys.data_ptr(), idxj.data_ptr(), vj.data_ptr(), self.nnz, keys.data_ptr(),
+                  None, None, None, None, J, lhs_d.data_ptr(), R, o.data_ptr(), I_j, st)
+        out[...] = o.cpu().numpy()

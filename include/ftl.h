@@ -155,6 +155,108 @@ int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples_dev,
                    double *h_dev, double *weights_dev, const double *draws_dev,
                    uint64_t seed, uint64_t ctr, void *stream);
 
+/* ------------------------------------------------ sparse tensors and CP-ALS */
+
+/* Fiber keys: keys_out[i] = mixed-radix number of the indices of every mode
+ * except j (first mode most significant; the product of the other modes'
+ * sizes must stay below 2^63), indices cast to uint32 first.  idx element
+ * (i, k) is at idx[i*stride_item + k*stride_mode], of type uint64 when
+ * idx_is_u64 else uint32 (nnz x N tensor indices: strides N, 1; an N x J
+ * sample array: strides 1, J).  The order of the keys is the lexicographic
+ * order of the reference's comparators on modes != j.
+ * Replaces the comparators of SortIdxLookup, cpp_ext/sort_lookup.hpp:49-59,
+ * and of the ALS dedup, cpp_ext/als.hpp:92-117. */
+int ftl_fiber_keys(const void *idx_dev, int idx_is_u64, int64_t n, int64_t stride_item,
+                   int64_t stride_mode, int N, const int64_t *dims, int j, uint64_t *keys_dev,
+                   void *stream);
+
+/* After sorting mode j's keys (perm = the sorting permutation): idxj_out[i] =
+ * idx[perm[i]*N + j], vals_out[i] = vals[perm[i]].  Replaces the sorted
+ * pointer array of SortIdxLookup, cpp_ext/sort_lookup.hpp:33-60. */
+int ftl_sparse_gather(const int64_t *perm_dev, const uint32_t *idx_dev, const double *vals_dev,
+                      int64_t nnz, int N, int j, uint32_t *idxj_out, double *vals_out, void *stream);
+
+/* Dedup of J sample keys: unique keys (slot order of a device hash table),
+ * the first sample index carrying each (rep) and its multiplicity (cnt);
+ * *num_unique_dev receives the count.  Replaces the sort / unique_copy /
+ * equal_range dedup of ALS::execute_ds_als_update, cpp_ext/als.hpp:83-153. */
+int ftl_dedup_workspace_bytes(int64_t J, size_t *out);
+int ftl_dedup(const uint64_t *keys_dev, int64_t J, void *workspace, size_t ws_bytes,
+              uint64_t *ukeys_dev, int32_t *urep_dev, int32_t *ucnt_dev,
+              int64_t *num_unique_dev, void *stream);
+
+/* gram_out (R x R, FP64) = sum over rows u of s_u lhs[row(u)] lhs[row(u)]^T,
+ * row(u) = rowidx ? rowidx[u] : u, s_u = (w ? w[row(u)] : 1) * (cnt ? cnt[u] : 1),
+ * u < (n_rows_dev ? *n_rows_dev : n_rows).  Deterministic (fixed-order
+ * reduction).  Replaces compute_pinv's Gram, cpp_ext/common.h:271-306, with
+ * the sqrt(w) row scaling of cpp_ext/als.hpp:155-160 folded in. */
+int ftl_gram_workspace_bytes(int R, size_t *out);
+int ftl_weighted_gram(const double *lhs_dev, const int32_t *rowidx_dev, const double *w_dev,
+                      const int32_t *cnt_dev, const int64_t *n_rows_dev, int64_t n_rows, int R,
+                      void *workspace, size_t ws_bytes, double *gram_out, void *stream);
+
+/* Pseudo-inverse of a symmetric R x R matrix (upper triangle read): keep
+ * eigenpair v (ascending) when v >= R - target and lambda_v > tol, target =
+ * min(*rank_cap_dev, R) when rank_cap_dev is given, else target_rank.
+ * vscratch (R*R FP64) is needed when R > 90.  Replaces compute_pinv_square,
+ * cpp_ext/common.h:228-269. */
+int ftl_pinv_square(const double *M_dev, int R, int target_rank, const int64_t *rank_cap_dev,
+                    double tol, double *out_dev, double *vscratch_dev, void *stream);
+
+/* Sparse MTTKRP through fiber lookup: out (I_j x R) is zeroed, then for every
+ * query q < (num_queries_dev ? *num_queries_dev : num_queries): the fiber of
+ * nonzeros whose mode-j-excluded key equals query_keys[q] is found by binary
+ * search in sorted_keys, and each of its nonzeros adds value * s_q *
+ * lhs[row(q)] to out[idx_j], row(q) = query_row ? query_row[q] : q,
+ * s_q = (w ? w[row(q)] : 1) * (cnt ? cnt[q] : 1).  Replaces
+ * SortIdxLookup::execute_spmm, cpp_ext/sort_lookup.hpp:69-132. */
+int ftl_sparse_mttkrp(const uint64_t *sorted_keys, const uint32_t *sorted_idxj,
+                      const double *sorted_vals, int64_t nnz, const uint64_t *query_keys,
+                      const int32_t *query_row, const double *w, const int32_t *cnt,
+                      const int64_t *num_queries_dev, int64_t num_queries, const double *lhs,
+                      int R, double *out, int64_t I_j, void *stream);
+
+/* U = B pinv row by row (pinv R x R symmetric); all-zero rows of B give zero
+ * rows without arithmetic.  Replaces the cblas_dsymm of
+ * cpp_ext/als.hpp:189-203. */
+int ftl_solve_rows(const double *B_dev, const double *pinv_dev, int64_t I, int R, double *U_dev,
+                   void *stream);
+
+/* Column norms of U (I x R) with norms <= 1e-7 replaced by 1, and (apply != 0)
+ * U /= norms.  Replaces LowRankTensor::renormalize_columns for one factor,
+ * cpp_ext/low_rank_tensor.hpp:203-247. */
+int ftl_colnorm_workspace_bytes(int R, size_t *out);
+int ftl_renormalize_columns(double *U_dev, int64_t I, int R, double *norms_out, void *workspace,
+                            size_t ws_bytes, int apply, void *stream);
+
+/* *out = sum over nonzeros of v^2 - 2 v model(idx), model = sum_r sigma_r
+ * prod_k U_k[idx_k, r] (the nonzero part of
+ * SortIdxLookup::compute_residual_normsq, cpp_ext/sort_lookup.hpp:134-193);
+ * U_dev is a host array of N device pointers. */
+int ftl_fit_workspace_bytes(size_t *out);
+int ftl_sparse_residual_terms(const uint32_t *idx_dev, const double *vals_dev, int64_t nnz, int N,
+                              const double *const *U_dev, const double *sigma_dev, int R,
+                              void *workspace, size_t ws_bytes, double *out_dev, void *stream);
+/* *out = sum of v_i^2 (SparseTensor's normsq, cpp_ext/sparse_tensor.hpp:70-74). */
+int ftl_sum_squares(const double *v_dev, int64_t n, void *workspace, size_t ws_bytes,
+                    double *out_dev, void *stream);
+
+/* Exact MTTKRP over all nonzeros: out[idx_j] += v prod_{k != j} U_k[idx_k]
+ * (out zeroed first).  Replaces SortIdxLookup::execute_exact_mttkrp,
+ * cpp_ext/sort_lookup.hpp:199-254. */
+int ftl_sparse_exact_mttkrp(const uint32_t *idx_dev, const double *vals_dev, int64_t nnz, int N,
+                            int j, const double *const *U_dev, int R, double *out_dev,
+                            int64_t I_j, void *stream);
+
+/* out_mat (R x R) = (sigma_a sigma_b^T) o prod_{k != exclude} G_k over N full
+ * R x R FP64 Grams (host array of device pointers; exclude = -1 for none; a
+ * NULL sigma means all ones); out_sum = sum of its entries.  Either output
+ * may be NULL.  Replaces ATB_chain_prod / ATB_chain_prod_sum with A = B,
+ * cpp_ext/common.h:152-226. */
+int ftl_gram_hadamard(const double *const *grams_dev, int N, int R, int exclude,
+                      const double *sigma_a, const double *sigma_b, double *out_mat,
+                      double *out_sum, void *stream);
+
 /* Size of the device array that ftl_krp_draw_static uses for scratch. */
 #define FTL_DRAW_STATIC_SCRATCH_BYTES (8u << 20)
 

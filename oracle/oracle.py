@@ -262,3 +262,93 @@ def krp_leverage(U_list, pinv_of=None):
     for u in U_list[1:]:
         rows = np.einsum("ir,jr->ijr", rows, u).reshape(-1, R)
     return np.einsum("ir,rs,is->i", rows, pinv, rows)
+
+
+# ------------------------------------------------------------------ CP-ALS
+
+def pinv_square(M: np.ndarray, target_rank: int, tol: float) -> np.ndarray:
+    """compute_pinv_square (cpp_ext/common.h:228-269): eigendecomposition of
+    the upper triangle, keep eigenpair v (ascending) when v >= R - target and
+    lambda_v > tol, return W W^T with W's kept columns v / sqrt(lambda_v)."""
+    R = M.shape[0]
+    lam, V = np.linalg.eigh(M, UPLO="U")
+    W = np.zeros((R, R))
+    for v in range(R):
+        if v >= R - target_rank and lam[v] > tol:
+            W[:, v] = V[:, v] / np.sqrt(lam[v])
+    return W @ W.T
+
+
+def fiber_keys(idx: np.ndarray, dims, j: int) -> np.ndarray:
+    """Mixed-radix key of the indices of the modes != j (first mode most
+    significant): the order of the reference's comparators on modes != j."""
+    N = idx.shape[1]
+    key = np.zeros(idx.shape[0], dtype=np.uint64)
+    for k in range(N):
+        if k == j:
+            continue
+        key = key * np.uint64(dims[k]) + idx[:, k].astype(np.uint64)
+    return key
+
+
+class OracleALS:
+    """ALS::execute_ds_als_update (cpp_ext/als.hpp:57-220) restated in numpy
+    over OracleKRPSampler, for a COO sparse tensor (SortIdxLookup semantics,
+    cpp_ext/sort_lookup.hpp:69-132)."""
+
+    def __init__(self, U_list, sigma, idx, vals, J: int, dims=None):
+        self.U = [np.array(u, dtype=np.float64, copy=True) for u in U_list]
+        self.N = len(self.U)
+        self.R = self.U[0].shape[1]
+        self.sigma = np.array(sigma, dtype=np.float64, copy=True)
+        self.idx = np.ascontiguousarray(idx, dtype=np.uint32)
+        self.vals = np.asarray(vals, dtype=np.float64)
+        self.dims = list(dims) if dims is not None else [u.shape[0] for u in self.U]
+        self.J = J
+        self.sampler = OracleKRPSampler(self.U, J, self.R)
+        self.lookups = []
+        for j in range(self.N):
+            k = fiber_keys(self.idx, self.dims, j)
+            perm = np.argsort(k, kind="stable")
+            self.lookups.append((k[perm], self.idx[perm, j].astype(np.int64), self.vals[perm]))
+
+    def update(self, j: int, draws, renormalize: bool = True, update_sampler: bool = True):
+        N, R, J = self.N, self.R, self.J
+        self.sampler.U = self.U
+        samples = self.sampler.draw(j, draws)
+        h, w = self.sampler.h, self.sampler.weights
+        T = samples.T.astype(np.uint32).astype(np.int64)          # als.hpp:76-81
+        keys = fiber_keys(T, self.dims, j)
+        uk, first, counts = np.unique(keys, return_index=True, return_counts=True)
+        wd = w[first] * counts                                      # :125-153
+        hd = h[first] * np.sqrt(wd)[:, None]                        # :155-160
+        pinv = pinv_square(hd.T @ hd, min(len(uk), R), 1e-11)       # :164-165
+        hd = hd * np.sqrt(wd)[:, None]                              # :169-174
+        skeys, sidx, svals = self.lookups[j]
+        lo = np.searchsorted(skeys, uk, side="left")
+        hi = np.searchsorted(skeys, uk, side="right")
+        out = np.zeros((self.U[j].shape[0], R))
+        for u in range(len(uk)):
+            for z in range(lo[u], hi[u]):
+                out[sidx[z]] += svals[z] * hd[u]
+        self.U[j] = out @ pinv                                      # :189-203
+        if renormalize:                                             # low_rank_tensor.hpp:203-260
+            norms = np.sqrt((self.U[j] ** 2).sum(axis=0))
+            norms[norms <= 1e-7] = 1.0
+            self.U[j] = self.U[j] / norms
+            self.sigma = norms
+        if update_sampler:
+            self.sampler.U[j] = self.U[j]
+            self.sampler.update_sampler(j)
+        self.last_samples = samples
+        return self.U[j]
+
+    def residual_normsq(self) -> float:
+        model = np.ones((self.idx.shape[0], self.R)) * self.sigma[None, :]
+        for k in range(self.N):
+            model = model * self.U[k][self.idx[:, k]]
+        m = model.sum(axis=1)
+        G = np.outer(self.sigma, self.sigma)
+        for k in range(self.N):
+            G = G * (self.U[k].T @ self.U[k])
+        return float(np.sum(self.vals ** 2 - 2 * self.vals * m) + G.sum())

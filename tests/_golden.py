@@ -29,3 +29,21 @@ def load_tree(name):
 
 def included_rows(N, j):
     return [k for k in range(N) if k != j]
+
+
+def als_cases():
+    return sorted(p.stem for p in GOLDEN.glob("als_*.npz"))
+
+
+def load_als(name):
+    z = np.load(GOLDEN / f"{name}.npz")
+    dims = [int(d) for d in z["dims"]]
+    N = len(dims)
+    c = dict(dims=dims, N=N, R=int(z["R"]), J=int(z["J"]), sweeps=int(z["sweeps"]), idx=z["idx"],
+             vals=z["vals"], sigma0=z["sigma0"], normsq=float(z["normsq"]),
+             U0=[z[f"U0_{k}"] for k in range(N)])
+    n_upd = c["sweeps"] * N
+    c["updates"] = [dict(j=u % N, draws=z[f"draws_{u}"], samples=z[f"samples_{u}"], U=z[f"U_{u}"],
+                         sigma=z[f"sigma_{u}"]) for u in range(n_upd)]
+    c["resid"] = [float(z[f"resid_{s}"]) for s in range(c["sweeps"])]
+    return c

@@ -49,6 +49,57 @@ def make_factors(rng, dims, R, heavy):
     return U
 
 
+# name: (dims, nnz, R, J, sweeps, seed)
+ALS_CASES = {
+    "als_sparse_3mode_r8": ([40, 30, 20], 2000, 8, 400, 2, 31),
+    "als_sparse_4mode_r5_ragged": ([17, 50, 9, 23], 1500, 5, 300, 2, 32),
+}
+
+
+def make_als_case(name, dims, nnz, R, J, sweeps, seed):
+    """Reference ALS (cpp_ext/als.hpp via the harness's InjectedALS): factors
+    renormalised once (renormalize_columns(-1), as the reference's benchmark
+    does), then `sweeps` sweeps of execute_ds_als_update(j, True, True) with
+    injected uniforms; records every update's samples and factor, and the
+    residual after each sweep."""
+    rng = np.random.default_rng(seed)
+    N = len(dims)
+    flat = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idx = np.stack(np.unravel_index(flat, dims), axis=1).astype(np.uint32)
+    vals = np.log1p(rng.lognormal(0.0, 1.0, size=nnz))
+    U = [rng.normal(size=(d, R)) for d in dims]
+    lr = ftl_ref.LowRankTensor(R, U)
+    lr.renormalize_columns(-1)
+    sigma0 = np.zeros(R)
+    lr.get_sigma(sigma0, -1)
+    out = {f"U0_{k}": U[k].copy() for k in range(N)}
+    sp = ftl_ref.SparseTensor(idx, vals, "sort")
+    als = ftl_ref.InjectedALS(lr, sp)
+    als.initialize_ds_als(J)
+    upd = 0
+    for sw in range(sweeps):
+        for j in range(N):
+            d = rng.random(2 * N * J)
+            als.set_draws(d)
+            als.execute_ds_als_update(j, True, True)
+            smp = np.zeros((N, J), dtype=np.uint64)
+            als.get_samples(smp)
+            sg = np.zeros(R)
+            lr.get_sigma(sg, -1)
+            out[f"draws_{upd}"] = d
+            out[f"samples_{upd}"] = smp
+            out[f"U_{upd}"] = U[j].copy()
+            out[f"sigma_{upd}"] = sg
+            upd += 1
+        sg = np.zeros(R)
+        lr.get_sigma(sg, -1)
+        out[f"resid_{sw}"] = np.array(sp.compute_residual_normsq(sg, U))
+    out.update(dims=np.array(dims), idx=idx, vals=vals, sigma0=sigma0, R=R, J=J, sweeps=sweeps,
+               normsq=np.array(sp.get_normsq()))
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "written")
+
+
 def main() -> None:
     for name, (N, dims, R, J, j, seed, heavy) in KRP_CASES.items():
         rng = np.random.default_rng(seed)
@@ -65,6 +116,8 @@ def main() -> None:
         out.update(N=N, R=R, J=J, j=j, draws=draws, samples=samples, h=h, weights=w)
         np.savez_compressed(HERE / f"{name}.npz", **out)
         print(name, "written")
+    for name, args in ALS_CASES.items():
+        make_als_case(name, *args)
     for name, (n, F, R, J, seed) in TREE_CASES.items():
         rng = np.random.default_rng(seed)
         U = rng.normal(size=(n, R))

@@ -1,0 +1,134 @@
+"""GPU parity of the randomized CP-ALS path against the reference's ALS
+(golden fixtures recorded from cpp_ext/als.hpp with injected uniforms) and
+the numpy ALS oracle.
+
+Tolerances: sampled indices identical (the trees are rebuilt from factors
+that agree to ~1e-13, so only near-ties could flip; none are allowed here);
+updated factors within 1e-9 of the largest entry; sigma and residuals within
+1e-9 relative; the CP fit (1 - ||X - model|| / ||X||) within 1e-6 relative,
+the target for the fit.  FP32 sampling: residual within 1e-3 relative of the
+FP64 trajectory.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests._golden import als_cases, load_als
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ftl():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fast_tensor_leverage_gb300 as m
+    return m
+
+
+def _setup(ftl, c, precision="fp64"):
+    U = [np.ascontiguousarray(u.copy()) for u in c["U0"]]
+    lr = ftl.LowRankTensor(c["R"], U)
+    lr.set_sigma(c["sigma0"])
+    sp = ftl.SparseTensor(c["idx"], c["vals"], "sort", dims=c["dims"])
+    als = ftl.ALS(lr, sp)
+    als.initialize_ds_als(c["J"], "efficient", precision=precision)
+    return U, lr, sp, als
+
+
+@pytest.mark.parametrize("name", als_cases())
+def test_gpu_als_matches_reference_golden(ftl, name):
+    c = load_als(name)
+    U, lr, sp, als = _setup(ftl, c)
+    assert abs(sp.get_normsq() - c["normsq"]) <= 1e-12 * c["normsq"]
+    N = c["N"]
+    for u, upd in enumerate(c["updates"]):
+        j = upd["j"]
+        als.execute_ds_als_update(j, True, True, draws=upd["draws"])
+        samples = als.sampler.samples_dev.cpu().numpy().view(np.uint64)
+        rows = [k for k in range(N) if k != j]
+        assert np.array_equal(samples[rows], upd["samples"][rows]), f"update {u}: samples differ"
+        # the host array is updated in place, like the reference's numpy factors
+        np.testing.assert_allclose(U[j], upd["U"], rtol=0, atol=1e-9 * np.abs(upd["U"]).max())
+        np.testing.assert_allclose(lr.sigma, upd["sigma"], rtol=1e-9)
+        if (u + 1) % N == 0:
+            resid = sp.compute_residual_normsq(lr.sigma_dev, lr.U_dev)
+            ref = c["resid"][u // N]
+            np.testing.assert_allclose(resid, ref, rtol=1e-9)
+            fit, fit_ref = 1 - np.sqrt(resid / c["normsq"]), 1 - np.sqrt(ref / c["normsq"])
+            assert abs(fit - fit_ref) <= 1e-6 * abs(fit_ref)
+
+
+def test_gpu_als_fp32_sampling_tracks_fp64(ftl):
+    c = load_als(als_cases()[0])
+    _, lr64, sp64, als64 = _setup(ftl, c, "fp64")
+    _, lr32, sp32, als32 = _setup(ftl, c, "fp32")
+    for upd in c["updates"]:
+        als64.execute_ds_als_update(upd["j"], True, True, draws=upd["draws"])
+        als32.execute_ds_als_update(upd["j"], True, True, draws=upd["draws"])
+    r64 = sp64.compute_residual_normsq(lr64.sigma_dev, lr64.U_dev)
+    r32 = sp32.compute_residual_normsq(lr32.sigma_dev, lr32.U_dev)
+    assert abs(r32 - r64) <= 1e-3 * r64
+
+
+def test_gpu_exact_als_update_matches_oracle(ftl):
+    c = load_als(als_cases()[0])
+    U, lr, sp, als = _setup(ftl, c)
+    Uo = [u.copy() for u in c["U0"]]
+    R = c["R"]
+    for j in range(c["N"]):
+        als.execute_exact_als_update(j, True, True)
+        # numpy restatement of execute_exact_als_update (cpp_ext/als.hpp:222-270)
+        G = np.ones((R, R))
+        for k in range(c["N"]):
+            if k != j:
+                G = G * (Uo[k].T @ Uo[k])
+        pinv = O.pinv_square(G, R, 1e-11)
+        mt = np.zeros_like(Uo[j])
+        part = c["vals"][:, None] * np.ones((1, R))
+        for k in range(c["N"]):
+            if k != j:
+                part = part * Uo[k][c["idx"][:, k]]
+        np.add.at(mt, c["idx"][:, j], part)
+        Uj = mt @ pinv
+        norms = np.sqrt((Uj ** 2).sum(axis=0))
+        norms[norms <= 1e-7] = 1.0
+        Uo[j] = Uj / norms
+        np.testing.assert_allclose(U[j], Uo[j], rtol=0, atol=1e-9 * np.abs(Uo[j]).max())
+        np.testing.assert_allclose(lr.sigma, norms, rtol=1e-9)
+
+
+def test_gpu_downsampled_mttkrp_and_norms(ftl):
+    c = load_als(als_cases()[1])
+    rng = np.random.default_rng(3)
+    sp = ftl.SparseTensor(c["idx"], c["vals"], "sort", dims=c["dims"])
+    N, R, J = c["N"], 7, 500
+    j = 2
+    samples = np.stack([rng.integers(0, d, size=J) for d in c["dims"]], axis=1).astype(np.uint64)
+    samples[: J // 2] = np.asarray(c["idx"][: J // 2], dtype=np.uint64)  # hit real fibers
+    lhs = rng.normal(size=(J, R))
+    out = np.zeros((c["dims"][j], R))
+    sp.execute_downsampled_mttkrp_py(samples, lhs, j, out)
+    keys = O.fiber_keys(c["idx"].astype(np.int64), c["dims"], j)
+    skeys = O.fiber_keys(samples.astype(np.int64), c["dims"], j)
+    ref = np.zeros_like(out)
+    for i in range(J):
+        for z in np.nonzero(keys == skeys[i])[0]:
+            ref[c["idx"][z, j]] += c["vals"][z] * lhs[i]
+    np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-12)
+    # LowRankTensor: renormalize every factor, sigma = product of norms
+    U = [rng.normal(size=(d, R)) for d in c["dims"]]
+    U0 = [u.copy() for u in U]
+    lr = ftl.LowRankTensor(R, U)
+    lr.renormalize_columns(-1)
+    prod = np.ones(R)
+    for k in range(N):
+        nk = np.sqrt((U0[k] ** 2).sum(axis=0))
+        prod *= nk
+        np.testing.assert_allclose(U[k], U0[k] / nk, rtol=1e-13)
+    np.testing.assert_allclose(lr.sigma, prod, rtol=1e-13)
+    G = np.outer(prod, prod)
+    for k in range(N):
+        G = G * (U[k].T @ U[k])
+    np.testing.assert_allclose(lr.get_normsq(), G.sum(), rtol=1e-11)
