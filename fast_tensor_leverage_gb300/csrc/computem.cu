@@ -75,7 +75,7 @@ __global__ void computem_pinv_kernel(CMParams p) {
         for (int e = tid; e < RR; e += nth) p.M[e] = p.M[(size_t)RR + e];
         __syncthreads();
     }
-    double *status = p.M + (size_t)(2 * N + 3) * RR;  // 1.0: Cholesky path taken
+    double *status = p.M + cm_status_offset(N, R);  // 1.0: Cholesky path taken
     bool chol = false;
     if (p.prec == FTL_PREC_FP32) {
         // Mixed mode: when every eigenvalue of M[0] exceeds the reference's
@@ -144,7 +144,7 @@ __global__ void computem_pinv_kernel(CMParams p) {
     }
     __syncthreads();
     }
-    double *pinv_packed = p.M + (size_t)(N + 1) * RR;
+    double *pinv_packed = p.M + cm_pinv64_offset(N, R);
     for (int e = tid; e < RR; e += nth) {
         p.M[e] = A[e];
         int a = e / R, b = e - a * R;
@@ -178,7 +178,7 @@ __global__ void computem_eig_kernel(CMParams p) {
     int *flag = order + R;
     const int offset = ((uint32_t)(k + 1) == p.j) ? k + 2 : k + 1;
     double *W = p.M + (size_t)offset * RR;
-    const bool chol = p.M[(size_t)(2 * N + 3) * RR] == 1.0;
+    const bool chol = p.M[cm_status_offset(N, R)] == 1.0;
     if (p.prec == FTL_PREC_FP32 && (offset < N || chol)) {
         // Mixed mode: FP32 Jacobi of M[offset] (offset < N), or of the FP64
         // pseudo-inverse when it came from the Cholesky path (offset == N;

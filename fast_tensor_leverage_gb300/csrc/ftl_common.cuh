@@ -21,6 +21,8 @@ int check_launch(const char *what);
         if (!(cond)) return ::ftl::fail(FTL_E_ARG, __VA_ARGS__);  \
     } while (0)
 
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 // ---------------------------------------------------------- tree geometry
 
 // Geometry of a PartitionTree over n rows with F rows per leaf.  Mirrors the
@@ -93,6 +95,14 @@ __host__ __device__ inline int node_stride(int R, int elem_bytes) {
     return (packed_size(R) + w - 1) / w * w;
 }
 __host__ __device__ inline int packed_row_offset(int a, int R) { return a * R - a * (a - 1) / 2; }
+
+// computeM workspace layout (doubles): 2N+3 dense R x R slots, one status
+// word, then the packed FP64 pseudo-inverse at a 16-byte aligned offset
+// (it is read with 16-byte vector loads), padded to its node stride.
+__host__ __device__ inline size_t cm_status_offset(int N, int R) { return (size_t)(2 * N + 3) * R * R; }
+__host__ __device__ inline size_t cm_pinv64_offset(int N, int R) {
+    return (cm_status_offset(N, R) + 1 + 1) / 2 * 2;
+}
 __host__ __device__ inline int packed_index(int a, int b, int R) {
     return packed_row_offset(a, R) + (b - a);
 }

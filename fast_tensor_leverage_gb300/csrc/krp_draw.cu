@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
             double scale = stage_query<RMAX, T>(h, R, xd, xT, lane);
             qf.setup(xT, pairs, lane);
             if (sizeof(T) == 8) {
-                double lev = (double)qf.eval((const T *)(p.M + (size_t)(p.N + 1) * RR), lane);
+                double lev = (double)qf.eval((const T *)(p.M + cm_pinv64_offset(p.N, R)), lane);
                 if (lane == 0) p.weights[i] = (double)R / (lev * (double)p.J);
             } else {
                 // w = R / (J lev), lev = lev_scaled / scale^2: the quotient in
@@ -260,9 +260,12 @@ static int validate_plan(const ftl_krp_plan *plan) {
     FTL_CHECK_ARG(plan->prec == FTL_PREC_FP64 || plan->prec == FTL_PREC_FP32, "krp: bad precision %d",
                   plan->prec);
     FTL_CHECK_ARG(plan->eig_G && plan->M && plan->lambda && plan->pinv32, "krp: null workspace pointer");
+    FTL_CHECK_ARG(aligned16(plan->eig_G) && aligned16(plan->M) && aligned16(plan->pinv32),
+                  "krp: eig_G, M and pinv32 must be 16-byte aligned");
     for (int k = 0; k < plan->N; ++k) {
         FTL_CHECK_ARG(plan->dims[k] >= 1, "krp: dims[%d]=%lld must be positive", k, (long long)plan->dims[k]);
         FTL_CHECK_ARG(plan->U[k] && plan->gram_G[k], "krp: null factor or tree pointer for mode %d", k);
+        FTL_CHECK_ARG(aligned16(plan->gram_G[k]), "krp: tree of mode %d must be 16-byte aligned", k);
     }
     return FTL_OK;
 }
@@ -282,9 +285,7 @@ extern "C" int ftl_krp_plan_sizes(int N, int R, int prec, size_t *eig_bytes, siz
     FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_krp_plan_sizes: bad precision");
     const int esize = prec == FTL_PREC_FP64 ? 8 : 4;
     if (eig_bytes) *eig_bytes = (size_t)N * (2 * R - 1) * node_stride(R, esize) * esize;
-    // slot N+1 holds the packed FP64 pseudo-inverse padded to its node stride,
-    // which can exceed R*R for R = 1: 16 spare doubles at the end
-    if (M_bytes) *M_bytes = ((size_t)(2 * N + 3) * R * R + 16) * sizeof(double);
+    if (M_bytes) *M_bytes = (cm_pinv64_offset(N, R) + node_stride(R, 8)) * sizeof(double);
     if (lambda_bytes) *lambda_bytes = (size_t)(N + 1) * R * sizeof(double);
     if (pinv32_bytes) *pinv32_bytes = (size_t)node_stride(R, 4) * sizeof(float);
     return FTL_OK;
@@ -353,6 +354,7 @@ extern "C" int ftl_tree_sample(const void *G, int prec, const double *U, int64_t
                                double *h, const double *scaled_h, uint64_t *samples,
                                const double *draws, int64_t J, void *stream) {
     FTL_CHECK_ARG(G && U && h && scaled_h && samples && draws, "ftl_tree_sample: null pointer");
+    FTL_CHECK_ARG(aligned16(G), "ftl_tree_sample: the tree must be 16-byte aligned");
     FTL_CHECK_ARG(n >= 1 && R >= 1 && R <= FTL_MAX_RANK && F >= 1 && F <= FTL_MAX_RANK && J >= 0,
                   "ftl_tree_sample: bad shape n=%lld R=%d F=%lld J=%lld (need R, F in [1, %d])",
                   (long long)n, R, (long long)F, (long long)J, FTL_MAX_RANK);

@@ -227,6 +227,7 @@ extern "C" int ftl_tree_build(const double *U, int64_t n, int R, int64_t F, int 
     FTL_CHECK_ARG(n >= 1 && F >= 1 && R >= 1 && R <= FTL_MAX_RANK,
                   "ftl_tree_build: bad shape n=%lld F=%lld R=%d", (long long)n, (long long)F, R);
     FTL_CHECK_ARG(F <= FTL_MAX_RANK, "ftl_tree_build: F=%lld exceeds %d", (long long)F, FTL_MAX_RANK);
+    FTL_CHECK_ARG(aligned16(G), "ftl_tree_build: the tree must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     if (prec == FTL_PREC_FP64) return build_impl<double>(U, n, R, F, (double *)G, st);
     if (prec == FTL_PREC_FP32) return build_impl<float>(U, n, R, F, (float *)G, st);

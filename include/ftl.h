@@ -75,8 +75,12 @@ typedef struct ftl_tree_geom {
  * cpp_ext/partition_tree.hpp:83-105 (log2_round_down: cpp_ext/common.h:21-33). */
 int ftl_tree_geometry(int64_t n, int64_t F, ftl_tree_geom *out);
 
-/* Bytes of one tree's node array: node_count * P * (8 for FP64, 4 for FP32). */
+/* Bytes of one tree's node array: node_count * node_stride * (8 for FP64, 4 for FP32). */
 int ftl_tree_bytes(int64_t n, int64_t F, int R, int prec, size_t *out_bytes);
+
+/* Node arrays (trees, eigen trees) and the computeM workspaces must be
+ * 16-byte aligned: nodes are read with 16-byte loads.  Each node occupies
+ * node_stride = P rounded up to 16 bytes (2 doubles / 4 floats), zero padded. */
 
 /* Build the node Grams of the tree over U_dev (n x R, FP64): each leaf holds
  * U_blk^T U_blk of its <= F rows, each internal node the sum of its children.

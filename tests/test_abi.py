@@ -56,6 +56,8 @@ def test_sizes():
     lambda: _lib.call("ftl_tree_build", 1, 10, 0, 8, 0, 1, None),
     lambda: _lib.call("ftl_tree_build", 1, 10, 129, 8, 0, 1, None),
     lambda: _lib.call("ftl_tree_build", 1, 10, 8, 8, 7, 1, None),
+    lambda: _lib.call("ftl_tree_build", 16, 10, 8, 8, 0, 24, None),   # unaligned tree
+    lambda: _lib.call("ftl_tree_sample", 24, 0, 16, 10, 8, 8, 16, 16, 16, 16, 5, None),
     lambda: _lib.call("ftl_tree_sample", 1, 0, 1, 10, 8, 0, 1, 1, 1, 1, 5, None),
     lambda: _lib.tree_geometry(0, 8),
     lambda: _lib.plan_sizes(0, 8, 0),

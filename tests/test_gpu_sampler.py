@@ -78,6 +78,8 @@ def test_fp64_draw_matches_reference_golden(ftl, name):
     (2, [600, 700], 128, 600, 3, 106),       # R = 128: eigenvectors in scratch
     (3, [20, 30, 40], 32, 1500, 4, 107),     # I < R: F = I, single-leaf trees
     (6, [50, 60, 70, 80, 90, 100], 16, 2000, 3, 108),
+    (4, [17, 50, 9, 23], 5, 1500, 2, 109),   # odd R with N + 1 odd: unaligned dense slots
+    (5, [33, 44, 55, 66, 77], 7, 1500, 6, 110),
 ])
 def test_fp64_draw_matches_oracle(ftl, N, dims, R, J, j, seed):
     rng = np.random.default_rng(seed)
@@ -128,6 +130,7 @@ def test_philox_stream_equals_injected_oracle_uniforms(ftl):
     (3, [4096, 2048, 3000], 32, 4000, 1),
     (2, [5000, 3000], 64, 2000, 3),
     (3, [20, 30, 40], 32, 3000, 4),   # rank-deficient Grams: Jacobi pseudo-inverse path
+    (4, [170, 500, 90, 230], 5, 3000, 1),
 ])
 def test_fp32_draw_agrees_with_fp64_oracle(ftl, N, dims, R, J, j):
     rng = np.random.default_rng(31 + R)
