@@ -160,20 +160,29 @@ class SparseTensor:
     def __init__(self, idx, vals, method: str = "sort", *, dims=None, device=None):
         if method != "sort":
             raise ValueError(f"Unknown lookup method {method!r} (only 'sort' is implemented)")
-        idx = np.asarray(idx)
-        if idx.ndim != 2 or idx.dtype != np.uint32:
-            raise TypeError("idx must be a (nnz, N) uint32 array")
-        vals = np.ascontiguousarray(np.asarray(vals, dtype=np.float64).reshape(-1))
-        if vals.shape[0] != idx.shape[0]:
-            raise ValueError("idx and vals disagree on nnz")
-        self.nnz, self.N = int(idx.shape[0]), int(idx.shape[1])
         self.device = D.cuda_device(device)
         dev = self.device
         st = D.stream_ptr(dev)
-        self.idx_dev = torch.from_numpy(np.ascontiguousarray(idx).view(np.int32)).to(dev)
-        self.vals_dev = torch.from_numpy(vals).to(dev)
-        if dims is None:
-            dims = (idx.max(axis=0).astype(np.int64) + 1) if self.nnz else np.ones(self.N, np.int64)
+        if isinstance(idx, torch.Tensor) and idx.is_cuda:
+            # device-resident input: (nnz, N) int32 holding the uint32 indices
+            if idx.dim() != 2 or idx.dtype != torch.int32:
+                raise TypeError("a CUDA idx must be a (nnz, N) int32 tensor")
+            self.idx_dev = idx.contiguous()
+            self.vals_dev = vals.to(dev, torch.float64).contiguous().reshape(-1)
+            if dims is None:
+                dims = (self.idx_dev.to(torch.int64).amax(dim=0) + 1).tolist()
+        else:
+            idx = np.asarray(idx)
+            if idx.ndim != 2 or idx.dtype != np.uint32:
+                raise TypeError("idx must be a (nnz, N) uint32 array")
+            v = np.ascontiguousarray(np.asarray(vals, dtype=np.float64).reshape(-1))
+            self.idx_dev = torch.from_numpy(np.ascontiguousarray(idx).view(np.int32)).to(dev)
+            self.vals_dev = torch.from_numpy(v).to(dev)
+            if dims is None:
+                dims = (idx.max(axis=0).astype(np.int64) + 1) if idx.shape[0] else np.ones(idx.shape[1], np.int64)
+        if self.vals_dev.shape[0] != self.idx_dev.shape[0]:
+            raise ValueError("idx and vals disagree on nnz")
+        self.nnz, self.N = int(self.idx_dev.shape[0]), int(self.idx_dev.shape[1])
         self.dims = [int(d) for d in dims]
         dims_c = (ctypes.c_int64 * self.N)(*self.dims)
         self._ws = _Workspace(dev)
