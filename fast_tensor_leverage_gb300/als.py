@@ -7,7 +7,8 @@ One sampled update of mode j (execute_ds_als_update, als.hpp:57-220):
   uint32-cast) -> dedup with multiplicities -> FP64 Gram of the
   sqrt(w * count)-scaled sampled KRP rows -> FP64 pseudo-inverse (rank cap
   min(unique, R), eigenvalue cut 1e-11) -> sparse MTTKRP of the
-  (w * count)-scaled rows through the sorted fiber lookup -> U_j = MTTKRP
+  (w * count)-scaled rows (one pass over the nonzeros grouped by output row,
+  probing the dedup hash table for each nonzero's fiber) -> U_j = MTTKRP
   pinv -> column renormalisation -> rebuild of mode j's partition tree.
 Every step is a kernel of libftl_gb300; the only host synchronisation is the
 optional mirror of the updated factor into the caller's numpy array.
@@ -92,11 +93,18 @@ class ALS:
         _lib.call("ftl_pinv_square", self._gram.data_ptr(), R, R, self._nuniq.data_ptr(), 1e-11,
                   self._pinv.data_ptr(), self._vscr.data_ptr(), st)
         I_j = lr.dims[j]
-        skeys, idxj, vj = gt.lookups[j]
         mt = self._mttkrp[: I_j * R]
-        _lib.call("ftl_sparse_mttkrp", skeys.data_ptr(), idxj.data_ptr(), vj.data_ptr(), gt.nnz,
-                  self._ukeys.data_ptr(), self._urep.data_ptr(), w.data_ptr(), self._ucnt.data_ptr(),
-                  self._nuniq.data_ptr(), J, h.data_ptr(), R, mt.data_ptr(), I_j, st)
+        if I_j == gt.dims[j]:
+            # one pass over the nonzeros grouped by output row, no atomics
+            row_ptr, rkeys, rvals = gt.rows[j]
+            _lib.call("ftl_sparse_mttkrp_rows", row_ptr.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), I_j,
+                      self._ws.get("dedup", nb).data_ptr(), J, self._urep.data_ptr(), self._ucnt.data_ptr(),
+                      w.data_ptr(), h.data_ptr(), R, mt.data_ptr(), st)
+        else:
+            skeys, idxj, vj = gt.lookups[j]
+            _lib.call("ftl_sparse_mttkrp", skeys.data_ptr(), idxj.data_ptr(), vj.data_ptr(), gt.nnz,
+                      self._ukeys.data_ptr(), self._urep.data_ptr(), w.data_ptr(), self._ucnt.data_ptr(),
+                      self._nuniq.data_ptr(), J, h.data_ptr(), R, mt.data_ptr(), I_j, st)
         _lib.call("ftl_solve_rows", mt.data_ptr(), self._pinv.data_ptr(), I_j, R, lr.U_dev[j].data_ptr(), st)
         if renormalize:
             lr.renormalize_columns(j)          # mirrors to the host array when lr.sync_host

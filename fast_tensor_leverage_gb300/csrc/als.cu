@@ -127,7 +127,8 @@ __global__ void table_insert_kernel(const uint64_t *__restrict__ skeys, int64_t 
 
 // Deterministic compaction in slot order (one CTA of 1024 threads).
 __global__ void table_compact_kernel(const uint64_t *keys, const int32_t *first, const int32_t *count, int64_t T,
-                                     uint64_t *ukeys, int32_t *urep, int32_t *ucnt, int64_t *num_unique) {
+                                     uint64_t *ukeys, int32_t *urep, int32_t *ucnt, int64_t *num_unique,
+                                     int32_t *slot_uidx) {
     __shared__ int warp_tot[32];
     __shared__ int64_t base_s;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -150,6 +151,7 @@ __global__ void table_compact_kernel(const uint64_t *keys, const int32_t *first,
             ukeys[o] = keys[s];
             urep[o] = first[s];
             ucnt[o] = count[s];
+            slot_uidx[s] = (int32_t)o;
         }
         __syncthreads();
         if (tid == 0) base_s += total;
@@ -308,6 +310,71 @@ __global__ void mttkrp_kernel(const uint64_t *__restrict__ skeys, const uint32_t
     }
 }
 
+// Row-driven MTTKRP (the same sum as mttkrp_kernel, grouped by output
+// row): nonzeros sorted by their mode-j index (CSR row_ptr), each carrying
+// its fiber key.  One warp per output row probes the dedup hash table for
+// every nonzero's fiber; a hit u adds v * w[rep_u] * cnt_u * h[rep_u] to the
+// row, accumulated in registers and written once -- no atomics, one pass
+// over the nonzeros.  Rows without hits are written as zeros.
+__global__ void mttkrp_rows_kernel(const int64_t *__restrict__ row_ptr, const uint64_t *__restrict__ rkeys,
+                                   const double *__restrict__ rvals, int64_t I_j,
+                                   const uint64_t *__restrict__ tkeys, const int32_t *__restrict__ slot_uidx,
+                                   int64_t T, const int32_t *__restrict__ urep, const int32_t *__restrict__ ucnt,
+                                   const double *__restrict__ w, const double *__restrict__ h, int R,
+                                   double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    constexpr int CPL = (FTL_MAX_RANK + 31) / 32;
+    for (int64_t row = gw; row < I_j; row += nw) {
+        double acc[CPL];
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) acc[c] = 0.0;
+        const int64_t z0 = row_ptr[row], z1 = row_ptr[row + 1];
+        for (int64_t zb = z0; zb < z1; zb += 32) {
+            const int64_t z = zb + lane;
+            int32_t u = -1;
+            double coef = 0.0;
+            if (z < z1) {
+                const uint64_t key = rkeys[z];
+                uint64_t s = mix64(key) & (uint64_t)(T - 1);
+                for (int64_t probe = 0; probe < T; ++probe) {
+                    const uint64_t k = tkeys[s];
+                    if (k == key) {
+                        u = slot_uidx[s];
+                        break;
+                    }
+                    if (k == kEmpty) break;
+                    s = (s + 1) & (uint64_t)(T - 1);
+                }
+                if (u >= 0) {
+                    const int32_t rep = urep[u];
+                    coef = rvals[z] * w[rep] * (double)ucnt[u];
+                    u = rep;
+                }
+            }
+            unsigned hits = __ballot_sync(0xffffffffu, u >= 0);
+            while (hits) {
+                const int src = __ffs(hits) - 1;
+                hits &= hits - 1;
+                const int32_t rep = __shfl_sync(0xffffffffu, u, src);
+                const double cf = __shfl_sync(0xffffffffu, coef, src);
+                const double *hr = h + (int64_t)rep * R;
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    const int col = lane + 32 * c;
+                    if (col < R) acc[c] = fma(cf, hr[col], acc[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+            const int col = lane + 32 * c;
+            if (col < R) out[row * R + col] = acc[c];
+        }
+    }
+}
+
 // ------------------------------------------------------ solve / renorm
 
 // U = B pinv (pinv R x R symmetric) row by row; an all-zero row of B (a row
@@ -375,10 +442,16 @@ __global__ void colnorm_finish_kernel(const double *__restrict__ partial, int nb
     }
 }
 
+// U /= norms per column, as a multiplication by the reciprocal (one rounding
+// more than the reference's division; an FP64 division per entry would cost
+// ~10x the FP64 issue of the multiply on this GPU).
 __global__ void colscale_kernel(double *__restrict__ U, int64_t I, int R, const double *__restrict__ norms) {
+    __shared__ double inv[FTL_MAX_RANK];
+    for (int c = threadIdx.x; c < R; c += blockDim.x) inv[c] = 1.0 / norms[c];
+    __syncthreads();
     const int64_t total = I * R;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
-        U[e] = U[e] / norms[e % R];
+        U[e] = U[e] * inv[e % R];
 }
 
 // ------------------------------------------------------------ fit terms
@@ -529,7 +602,7 @@ extern "C" int ftl_sparse_gather(const int64_t *perm, const uint32_t *idx, const
 
 extern "C" int ftl_dedup_workspace_bytes(int64_t J, size_t *out) {
     FTL_CHECK_ARG(out && J >= 1 && J <= INT32_MAX / 2, "ftl_dedup_workspace_bytes: bad J=%lld", (long long)J);
-    *out = (size_t)table_size_for(J) * (sizeof(uint64_t) + 2 * sizeof(int32_t));
+    *out = (size_t)table_size_for(J) * (sizeof(uint64_t) + 3 * sizeof(int32_t));
     return FTL_OK;
 }
 
@@ -544,11 +617,28 @@ extern "C" int ftl_dedup(const uint64_t *keys, int64_t J, void *workspace, size_
     uint64_t *tk = (uint64_t *)workspace;
     int32_t *tf = (int32_t *)(tk + T);
     int32_t *tc = tf + T;
+    int32_t *tu = tc + T;
     cudaStream_t st = (cudaStream_t)stream;
     table_clear_kernel<<<grid_for(T), 256, 0, st>>>(tk, tf, tc, T);
     table_insert_kernel<<<grid_for(J), 256, 0, st>>>(keys, J, tk, tf, tc, T);
-    table_compact_kernel<<<1, 1024, 0, st>>>(tk, tf, tc, T, ukeys, urep, ucnt, num_unique);
+    table_compact_kernel<<<1, 1024, 0, st>>>(tk, tf, tc, T, ukeys, urep, ucnt, num_unique, tu);
     return check_launch("dedup kernels");
+}
+
+extern "C" int ftl_sparse_mttkrp_rows(const int64_t *row_ptr, const uint64_t *row_keys, const double *row_vals,
+                                      int64_t I_j, const void *dedup_workspace, int64_t J, const int32_t *urep,
+                                      const int32_t *ucnt, const double *w, const double *h, int R, double *out,
+                                      void *stream) {
+    FTL_CHECK_ARG(row_ptr && row_keys && row_vals && dedup_workspace && urep && ucnt && w && h && out,
+                  "ftl_sparse_mttkrp_rows: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1 && J >= 1, "ftl_sparse_mttkrp_rows: bad shape");
+    const int64_t T = table_size_for(J);
+    const uint64_t *tk = (const uint64_t *)dedup_workspace;
+    const int32_t *tu = (const int32_t *)(tk + T) + 2 * T;
+    int blocks = (int)std::min<int64_t>((I_j * 32 + 255) / 256, (int64_t)num_sms() * 16);
+    mttkrp_rows_kernel<<<std::max(blocks, 1), 256, 0, (cudaStream_t)stream>>>(row_ptr, row_keys, row_vals, I_j, tk,
+                                                                             tu, T, urep, ucnt, w, h, R, out);
+    return check_launch("mttkrp_rows_kernel");
 }
 
 extern "C" int ftl_gram_workspace_bytes(int R, size_t *out) {

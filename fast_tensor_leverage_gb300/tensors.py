@@ -186,20 +186,27 @@ class SparseTensor:
         self.dims = [int(d) for d in dims]
         dims_c = (ctypes.c_int64 * self.N)(*self.dims)
         self._ws = _Workspace(dev)
-        self.lookups = []
+        self.lookups = []   # per mode: fiber keys sorted, their mode-j index and value
+        self.rows = []      # per mode: CSR over the mode-j index with each nonzero's fiber key
         for j in range(self.N):
             keys = torch.empty(self.nnz, dtype=torch.int64, device=dev)
             _lib.call("ftl_fiber_keys", self.idx_dev.data_ptr(), 0, self.nnz, self.N, 1, self.N, dims_c, j,
                       keys.data_ptr(), st)
-            # one-off construction sort of the fiber keys (keys < 2^63, so the
-            # signed order is the unsigned order)
+            # one-off construction sorts (keys < 2^63, so the signed order is
+            # the unsigned order)
             skeys, perm = torch.sort(keys)
             idxj = torch.empty(self.nnz, dtype=torch.int32, device=dev)
             vj = torch.empty(self.nnz, dtype=torch.float64, device=dev)
             _lib.call("ftl_sparse_gather", perm.data_ptr(), self.idx_dev.data_ptr(), self.vals_dev.data_ptr(),
                       self.nnz, self.N, j, idxj.data_ptr(), vj.data_ptr(), st)
-            del perm, keys
+            del perm
             self.lookups.append((skeys, idxj, vj))
+            col = self.idx_dev[:, j].to(torch.int64)
+            rperm = torch.argsort(col, stable=True)
+            row_ptr = torch.zeros(self.dims[j] + 1, dtype=torch.int64, device=dev)
+            row_ptr[1:] = torch.cumsum(torch.bincount(col, minlength=self.dims[j]), 0)
+            self.rows.append((row_ptr, keys[rperm].contiguous(), self.vals_dev[rperm].contiguous()))
+            del keys, rperm, col
         nb = _lib.ws_bytes("fit")
         out = torch.empty(1, dtype=torch.float64, device=dev)
         _lib.call("ftl_sum_squares", self.vals_dev.data_ptr(), self.nnz, self._ws.get("fit", nb).data_ptr(), nb,

@@ -220,6 +220,16 @@ int ftl_sparse_mttkrp(const uint64_t *sorted_keys, const uint32_t *sorted_idxj,
                       const int64_t *num_queries_dev, int64_t num_queries, const double *lhs,
                       int R, double *out, int64_t I_j, void *stream);
 
+/* The same MTTKRP grouped by output row: nonzeros sorted by their mode-j
+ * index (CSR row_ptr, I_j + 1 entries) with their fiber keys row_keys and
+ * values row_vals; queries are the unique fibers of the last ftl_dedup on
+ * dedup_workspace (sized for J).  One pass over the nonzeros, every output
+ * row written once (no atomics); out needs no zeroing. */
+int ftl_sparse_mttkrp_rows(const int64_t *row_ptr, const uint64_t *row_keys,
+                           const double *row_vals, int64_t I_j, const void *dedup_workspace,
+                           int64_t J, const int32_t *urep, const int32_t *ucnt, const double *w,
+                           const double *h, int R, double *out, void *stream);
+
 /* U = B pinv row by row (pinv R x R symmetric); all-zero rows of B give zero
  * rows without arithmetic.  Replaces the cblas_dsymm of
  * cpp_ext/als.hpp:189-203. */
@@ -227,7 +237,7 @@ int ftl_solve_rows(const double *B_dev, const double *pinv_dev, int64_t I, int R
                    void *stream);
 
 /* Column norms of U (I x R) with norms <= 1e-7 replaced by 1, and (apply != 0)
- * U /= norms.  Replaces LowRankTensor::renormalize_columns for one factor,
+ * U *= 1/norms (the reference divides; this differs by at most one rounding).  Replaces LowRankTensor::renormalize_columns for one factor,
  * cpp_ext/low_rank_tensor.hpp:203-247. */
 int ftl_colnorm_workspace_bytes(int R, size_t *out);
 int ftl_renormalize_columns(double *U_dev, int64_t I, int R, double *norms_out, void *workspace,
