@@ -87,7 +87,7 @@ SIGNATURES = {
     "ftl_weighted_gram": ([_P, _P, _P, _P, _P, _I64, _INT, _P, ctypes.c_size_t, _P, _P], _INT),
     "ftl_pinv_square": ([_P, _INT, _INT, _P, ctypes.c_double, _P, _P, _P], _INT),
     "ftl_sparse_mttkrp": ([_P, _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _INT, _P, _I64, _P], _INT),
-    "ftl_sparse_mttkrp_rows": ([_P, _P, _P, _I64, _P, _I64, _P, _P, _P, _P, _INT, _P, _P], _INT),
+    "ftl_sparse_mttkrp_rows": ([_P, _P, _P, _I64, _P, _I64, _P, _P, _P, _P, _INT, _P, _I64, _P], _INT),
     "ftl_solve_rows": ([_P, _P, _I64, _INT, _P, _P], _INT),
     "ftl_colnorm_workspace_bytes": ([_INT, _SZP], _INT),
     "ftl_renormalize_columns": ([_P, _I64, _INT, _P, _P, ctypes.c_size_t, _INT, _P], _INT),

@@ -7,8 +7,9 @@ One sampled update of mode j (execute_ds_als_update, als.hpp:57-220):
   uint32-cast) -> dedup with multiplicities -> FP64 Gram of the
   sqrt(w * count)-scaled sampled KRP rows -> FP64 pseudo-inverse (rank cap
   min(unique, R), eigenvalue cut 1e-11) -> sparse MTTKRP of the
-  (w * count)-scaled rows (one pass over the nonzeros grouped by output row,
-  probing the dedup hash table for each nonzero's fiber) -> U_j = MTTKRP
+  (w * count)-scaled rows (one balanced pass over the nonzeros sorted by
+  output row, probing the dedup hash table for each nonzero's fiber) ->
+  U_j = MTTKRP
   pinv -> column renormalisation -> rebuild of mode j's partition tree.
 Every step is a kernel of libftl_gb300; the only host synchronisation is the
 optional mirror of the updated factor into the caller's numpy array.
@@ -95,11 +96,11 @@ class ALS:
         I_j = lr.dims[j]
         mt = self._mttkrp[: I_j * R]
         if I_j == gt.dims[j]:
-            # one pass over the nonzeros grouped by output row, no atomics
-            row_ptr, rkeys, rvals = gt.rows[j]
-            _lib.call("ftl_sparse_mttkrp_rows", row_ptr.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), I_j,
+            # one balanced pass over the nonzeros sorted by output row
+            rrows, rkeys, rvals = gt.rows[j]
+            _lib.call("ftl_sparse_mttkrp_rows", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), gt.nnz,
                       self._ws.get("dedup", nb).data_ptr(), J, self._urep.data_ptr(), self._ucnt.data_ptr(),
-                      w.data_ptr(), h.data_ptr(), R, mt.data_ptr(), st)
+                      w.data_ptr(), h.data_ptr(), R, mt.data_ptr(), I_j, st)
         else:
             skeys, idxj, vj = gt.lookups[j]
             _lib.call("ftl_sparse_mttkrp", skeys.data_ptr(), idxj.data_ptr(), vj.data_ptr(), gt.nnz,

@@ -310,14 +310,18 @@ __global__ void mttkrp_kernel(const uint64_t *__restrict__ skeys, const uint32_t
     }
 }
 
-// Row-driven MTTKRP (the same sum as mttkrp_kernel, grouped by output
-// row): nonzeros sorted by their mode-j index (CSR row_ptr), each carrying
-// its fiber key.  One warp per output row probes the dedup hash table for
-// every nonzero's fiber; a hit u adds v * w[rep_u] * cnt_u * h[rep_u] to the
-// row, accumulated in registers and written once -- no atomics, one pass
-// over the nonzeros.  Rows without hits are written as zeros.
-__global__ void mttkrp_rows_kernel(const int64_t *__restrict__ row_ptr, const uint64_t *__restrict__ rkeys,
-                                   const double *__restrict__ rvals, int64_t I_j,
+// Row-grouped MTTKRP (the same sum as mttkrp_kernel): nonzeros sorted by
+// their mode-j index, each carrying its row and fiber key.  The sorted
+// nonzeros are cut into fixed chunks of MTT_CHUNK, one warp per chunk, so
+// work is balanced however skewed the rows are.  Lanes probe the dedup hash
+// table for 32 nonzeros at a time; hits are applied in nonzero order to a
+// per-row accumulator (lane = column) that is flushed with one atomic add
+// per column whenever the row changes -- a handful of atomics per chunk
+// instead of R per touched nonzero.
+constexpr int MTT_CHUNK = 512;
+
+__global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
+                                   const double *__restrict__ rvals, int64_t nnz,
                                    const uint64_t *__restrict__ tkeys, const int32_t *__restrict__ slot_uidx,
                                    int64_t T, const int32_t *__restrict__ urep, const int32_t *__restrict__ ucnt,
                                    const double *__restrict__ w, const double *__restrict__ h, int R,
@@ -326,18 +330,21 @@ __global__ void mttkrp_rows_kernel(const int64_t *__restrict__ row_ptr, const ui
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     constexpr int CPL = (FTL_MAX_RANK + 31) / 32;
-    for (int64_t row = gw; row < I_j; row += nw) {
+    const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
+    for (int64_t ch = gw; ch < nchunks; ch += nw) {
+        const int64_t z0 = ch * MTT_CHUNK, z1 = min(nnz, z0 + MTT_CHUNK);
         double acc[CPL];
 #pragma unroll
         for (int c = 0; c < CPL; ++c) acc[c] = 0.0;
-        const int64_t z0 = row_ptr[row], z1 = row_ptr[row + 1];
+        int32_t cur = -1;  // row held in acc (warp-uniform)
         for (int64_t zb = z0; zb < z1; zb += 32) {
             const int64_t z = zb + lane;
-            int32_t u = -1;
+            int32_t rep = -1, row = -1;
             double coef = 0.0;
             if (z < z1) {
                 const uint64_t key = rkeys[z];
                 uint64_t s = mix64(key) & (uint64_t)(T - 1);
+                int32_t u = -1;
                 for (int64_t probe = 0; probe < T; ++probe) {
                     const uint64_t k = tkeys[s];
                     if (k == key) {
@@ -348,18 +355,30 @@ __global__ void mttkrp_rows_kernel(const int64_t *__restrict__ row_ptr, const ui
                     s = (s + 1) & (uint64_t)(T - 1);
                 }
                 if (u >= 0) {
-                    const int32_t rep = urep[u];
+                    rep = urep[u];
+                    row = rrows[z];
                     coef = rvals[z] * w[rep] * (double)ucnt[u];
-                    u = rep;
                 }
             }
-            unsigned hits = __ballot_sync(0xffffffffu, u >= 0);
+            unsigned hits = __ballot_sync(0xffffffffu, rep >= 0);
             while (hits) {
                 const int src = __ffs(hits) - 1;
                 hits &= hits - 1;
-                const int32_t rep = __shfl_sync(0xffffffffu, u, src);
+                const int32_t hrep = __shfl_sync(0xffffffffu, rep, src);
+                const int32_t hrow = __shfl_sync(0xffffffffu, row, src);
                 const double cf = __shfl_sync(0xffffffffu, coef, src);
-                const double *hr = h + (int64_t)rep * R;
+                if (hrow != cur) {
+                    if (cur >= 0) {
+#pragma unroll
+                        for (int c = 0; c < CPL; ++c) {
+                            const int col = lane + 32 * c;
+                            if (col < R) atomicAdd(out + (int64_t)cur * R + col, acc[c]);
+                            acc[c] = 0.0;
+                        }
+                    }
+                    cur = hrow;
+                }
+                const double *hr = h + (int64_t)hrep * R;
 #pragma unroll
                 for (int c = 0; c < CPL; ++c) {
                     const int col = lane + 32 * c;
@@ -367,10 +386,12 @@ __global__ void mttkrp_rows_kernel(const int64_t *__restrict__ row_ptr, const ui
                 }
             }
         }
+        if (cur >= 0) {
 #pragma unroll
-        for (int c = 0; c < CPL; ++c) {
-            const int col = lane + 32 * c;
-            if (col < R) out[row * R + col] = acc[c];
+            for (int c = 0; c < CPL; ++c) {
+                const int col = lane + 32 * c;
+                if (col < R) atomicAdd(out + (int64_t)cur * R + col, acc[c]);
+            }
         }
     }
 }
@@ -625,19 +646,24 @@ extern "C" int ftl_dedup(const uint64_t *keys, int64_t J, void *workspace, size_
     return check_launch("dedup kernels");
 }
 
-extern "C" int ftl_sparse_mttkrp_rows(const int64_t *row_ptr, const uint64_t *row_keys, const double *row_vals,
-                                      int64_t I_j, const void *dedup_workspace, int64_t J, const int32_t *urep,
+extern "C" int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *row_keys, const double *row_vals,
+                                      int64_t nnz, const void *dedup_workspace, int64_t J, const int32_t *urep,
                                       const int32_t *ucnt, const double *w, const double *h, int R, double *out,
-                                      void *stream) {
-    FTL_CHECK_ARG(row_ptr && row_keys && row_vals && dedup_workspace && urep && ucnt && w && h && out,
+                                      int64_t I_j, void *stream) {
+    FTL_CHECK_ARG(row_idx && row_keys && row_vals && dedup_workspace && urep && ucnt && w && h && out,
                   "ftl_sparse_mttkrp_rows: null pointer");
-    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1 && J >= 1, "ftl_sparse_mttkrp_rows: bad shape");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1 && J >= 1 && nnz >= 0, "ftl_sparse_mttkrp_rows: bad shape");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t err = cudaMemsetAsync(out, 0, (size_t)I_j * R * sizeof(double), st);
+    if (err != cudaSuccess) return fail(FTL_E_CUDA, "ftl_sparse_mttkrp_rows: memset: %s", cudaGetErrorString(err));
+    if (nnz == 0) return FTL_OK;
     const int64_t T = table_size_for(J);
     const uint64_t *tk = (const uint64_t *)dedup_workspace;
     const int32_t *tu = (const int32_t *)(tk + T) + 2 * T;
-    int blocks = (int)std::min<int64_t>((I_j * 32 + 255) / 256, (int64_t)num_sms() * 16);
-    mttkrp_rows_kernel<<<std::max(blocks, 1), 256, 0, (cudaStream_t)stream>>>(row_ptr, row_keys, row_vals, I_j, tk,
-                                                                             tu, T, urep, ucnt, w, h, R, out);
+    const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
+    int blocks = (int)std::min<int64_t>((nchunks * 32 + 255) / 256, (int64_t)num_sms() * 32);
+    mttkrp_rows_kernel<<<std::max(blocks, 1), 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep,
+                                                             ucnt, w, h, R, out);
     return check_launch("mttkrp_rows_kernel");
 }
 

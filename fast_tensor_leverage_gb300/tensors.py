@@ -187,7 +187,7 @@ class SparseTensor:
         dims_c = (ctypes.c_int64 * self.N)(*self.dims)
         self._ws = _Workspace(dev)
         self.lookups = []   # per mode: fiber keys sorted, their mode-j index and value
-        self.rows = []      # per mode: CSR over the mode-j index with each nonzero's fiber key
+        self.rows = []      # per mode: nonzeros sorted by mode-j index (index, fiber key, value)
         for j in range(self.N):
             keys = torch.empty(self.nnz, dtype=torch.int64, device=dev)
             _lib.call("ftl_fiber_keys", self.idx_dev.data_ptr(), 0, self.nnz, self.N, 1, self.N, dims_c, j,
@@ -201,11 +201,9 @@ class SparseTensor:
                       self.nnz, self.N, j, idxj.data_ptr(), vj.data_ptr(), st)
             del perm
             self.lookups.append((skeys, idxj, vj))
-            col = self.idx_dev[:, j].to(torch.int64)
+            col = self.idx_dev[:, j]
             rperm = torch.argsort(col, stable=True)
-            row_ptr = torch.zeros(self.dims[j] + 1, dtype=torch.int64, device=dev)
-            row_ptr[1:] = torch.cumsum(torch.bincount(col, minlength=self.dims[j]), 0)
-            self.rows.append((row_ptr, keys[rperm].contiguous(), self.vals_dev[rperm].contiguous()))
+            self.rows.append((col[rperm].contiguous(), keys[rperm].contiguous(), self.vals_dev[rperm].contiguous()))
             del keys, rperm, col
         nb = _lib.ws_bytes("fit")
         out = torch.empty(1, dtype=torch.float64, device=dev)

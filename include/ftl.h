@@ -221,14 +221,15 @@ int ftl_sparse_mttkrp(const uint64_t *sorted_keys, const uint32_t *sorted_idxj,
                       int R, double *out, int64_t I_j, void *stream);
 
 /* The same MTTKRP grouped by output row: nonzeros sorted by their mode-j
- * index (CSR row_ptr, I_j + 1 entries) with their fiber keys row_keys and
- * values row_vals; queries are the unique fibers of the last ftl_dedup on
- * dedup_workspace (sized for J).  One pass over the nonzeros, every output
- * row written once (no atomics); out needs no zeroing. */
-int ftl_sparse_mttkrp_rows(const int64_t *row_ptr, const uint64_t *row_keys,
-                           const double *row_vals, int64_t I_j, const void *dedup_workspace,
+ * index, given as row_idx (that index), row_keys (fiber keys) and row_vals;
+ * queries are the unique fibers of the last ftl_dedup on dedup_workspace
+ * (sized for J).  One pass over the nonzeros in fixed chunks (balanced under
+ * any row skew), per-row accumulation, one atomic add per row segment; out
+ * (I_j x R) is zeroed first. */
+int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *row_keys,
+                           const double *row_vals, int64_t nnz, const void *dedup_workspace,
                            int64_t J, const int32_t *urep, const int32_t *ucnt, const double *w,
-                           const double *h, int R, double *out, void *stream);
+                           const double *h, int R, double *out, int64_t I_j, void *stream);
 
 /* U = B pinv row by row (pinv R x R symmetric); all-zero rows of B give zero
  * rows without arithmetic.  Replaces the cblas_dsymm of
