@@ -96,6 +96,8 @@ SIGNATURES = {
     "ftl_sum_squares": ([_P, _I64, _P, ctypes.c_size_t, _P, _P], _INT),
     "ftl_sparse_exact_mttkrp": ([_P, _P, _I64, _INT, _INT, _P, _INT, _P, _I64, _P], _INT),
     "ftl_gram_hadamard": ([_P, _INT, _INT, _INT, _P, _P, _P, _P, _P], _INT),
+    "ftl_krp_sample_packed": ([_P, _INT, _P, _P, _P, _P, _P, _P, _P, _P], _INT),
+    "ftl_philox_uniforms_dev": ([_P, _I64, _U64, _P, _P], _INT),
     "ftl_philox_uniforms": ([_P, _I64, _U64, _U64, _P], _INT),
 }
 

@@ -142,6 +142,55 @@ class ALS:
     def num_unique_samples(self) -> int:
         return int(self._nuniq.item())
 
+    # ------------------------------------------------------- captured sweeps
+    def capture_sweep(self, renormalize: bool = True, update_sampler: bool = True) -> None:
+        """Capture one sweep (a sampled update of every mode) as a CUDA
+        graph.  Its uniforms come from the Philox stream of the sampler's seed
+        at a device-resident counter that the graph advances, so every replay
+        draws fresh samples -- the same uniforms the eager updates would use
+        from the current counter on.  The decomposition must keep its factors
+        on the device (sync_host=False)."""
+        if self.sampler is None:
+            raise RuntimeError("initialize_ds_als must be called first")
+        lr = self.cp_decomp
+        if lr.sync_host:
+            raise RuntimeError("graph capture needs LowRankTensor(..., sync_host=False)")
+        N, J = lr.N, self.J
+        dev = self.device
+        self._ctr_dev = torch.tensor([self.sampler.counter], dtype=torch.int64, device=dev)
+        self._gdraws = torch.empty(2 * N * J, dtype=torch.float64, device=dev)
+
+        def sweep():
+            st = D.stream_ptr(dev)
+            for j in range(N):
+                _lib.call("ftl_philox_uniforms_dev", self._gdraws.data_ptr(), 2 * N * J, self.sampler.seed,
+                          self._ctr_dev.data_ptr(), st)
+                self.execute_ds_als_update(j, renormalize, update_sampler, draws=self._gdraws)
+
+        # warm-up on a side stream settles workspaces and kernel attributes,
+        # then restore the state it advanced
+        saved = [u.clone() for u in lr.U_dev] + [lr.sigma_dev.clone(), self._ctr_dev.clone()]
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            sweep()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        for t, v in zip(lr.U_dev + [lr.sigma_dev, self._ctr_dev], saved):
+            t.copy_(v)
+        for j in range(N):
+            self.sampler.update_sampler(j)
+        torch.cuda.synchronize(dev)
+        self._graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self._graph):
+            sweep()
+
+    def replay_sweep(self) -> None:
+        """Run one captured sweep on the current stream."""
+        self._graph.replay()
+        # keep the host copy of the Philox counter in step with the device one
+        N, J = self.cp_decomp.N, self.J
+        self.sampler.counter += N * 2 * N * J
+
 
 # ------------------------------------------------------------ Python driver
 

@@ -41,94 +41,148 @@ __device__ __forceinline__ double get_draw(const DrawParams &p, int64_t idx) {
     return p.draws ? p.draws[idx] : philox_uniform(p.seed, p.ctr + (uint64_t)idx);
 }
 
+// Per-warp state of the draw kernels: the block's pair table and the warp's
+// shared-memory slot.
 template <int RMAX, typename T>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
-    using S = Shape<RMAX>;
-    constexpr int XPL = S::XPL;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+struct DrawWarp {
+    const uint16_t *pairs;
+    double *xd;
+    T *xT;
+    QForm<RMAX, T> qf;
+    int lane;
+};
+
+template <int RMAX, typename T>
+__device__ __forceinline__ void setup_draw_warp(DrawWarp<RMAX, T> &dw, unsigned char *smem_raw, int R, int P, int S) {
     uint16_t *pairs = (uint16_t *)smem_raw;
-    const int R = p.R, P = p.P;
     build_pairs(pairs, R);
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     unsigned char *slot = smem_raw + ((NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16) +
                           warp * WarpSlot<RMAX, T>::bytes;
-    double *xd = (double *)slot;
-    T *xT = sizeof(T) == 8 ? (T *)xd : (T *)(xd + RMAX);
-    QForm<RMAX, T> qf;
-    qf.P = P;
-    qf.S = p.S;
-    qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
+    dw.pairs = pairs;
+    dw.xd = (double *)slot;
+    dw.xT = sizeof(T) == 8 ? (T *)dw.xd : (T *)(dw.xd + RMAX);
+    dw.qf.P = P;
+    dw.qf.S = S;
+    dw.qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
+    dw.lane = threadIdx.x & 31;
+}
+
+// Sample i of one draw: for every included mode the eigen-component descent
+// and the Gram-tree descent, then the weight and the row of h.
+template <int RMAX, typename T>
+__device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, DrawWarp<RMAX, T> &dw) {
+    using S = Shape<RMAX>;
+    constexpr int XPL = S::XPL;
+    const int R = p.R;
+    const int lane = dw.lane;
+    const uint16_t *pairs = dw.pairs;
+    double *xd = dw.xd;
+    T *xT = dw.xT;
+    QForm<RMAX, T> &qf = dw.qf;
     const size_t RR = (size_t)R * R;
     const size_t eig_stride = (size_t)(2 * R - 1) * p.S;
     const float RJ = (float)((double)R / (double)p.J);
-
-    for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
-         i += (int64_t)gridDim.x * S::WARPS) {
-        double h[XPL];
+    double h[XPL];
 #pragma unroll
-        for (int q = 0; q < XPL; ++q) h[q] = 1.0;
+    for (int q = 0; q < XPL; ++q) h[q] = 1.0;
 #pragma unroll 1
-        for (int k = 0; k < p.N; ++k) {
-            if ((uint32_t)k == p.j) continue;
-            // phase 0: eigen-component descent, query h;
-            // phase 1: Gram-tree descent, query h o W[u], leaf scan, h o= U_k[t]
-            double x[XPL];
+    for (int k = 0; k < p.N; ++k) {
+        if ((uint32_t)k == p.j) continue;
+        // phase 0: eigen-component descent, query h;
+        // phase 1: Gram-tree descent, query h o W[u], leaf scan, h o= U_k[t]
+        double x[XPL];
 #pragma unroll
-            for (int q = 0; q < XPL; ++q) x[q] = h[q];
+        for (int q = 0; q < XPL; ++q) x[q] = h[q];
 #pragma unroll 1
-            for (int phase = 0; phase < 2; ++phase) {
-                const T *G = phase == 0 ? (const T *)p.eig_G + k * eig_stride : (const T *)p.gram_G[k];
-                const DGeom &g = phase == 0 ? p.eig : p.gram[k];
-                const double *Uk = p.U[k];
-                __syncwarp();
-                stage_query<RMAX, T>(x, R, xd, xT, lane);
-                qf.setup(xT, pairs, lane);
-                T frac;
-                const int64_t c = descend<RMAX>(G, p.S, g, get_draw(p, (int64_t)(phase * p.N + k) * p.J + i),
-                                                qf, lane, frac, (phase == 1 && g.F > 1) ? Uk : nullptr, R);
-                if (phase == 0) {
-                    const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)leaf_index(g, c) * R;
-#pragma unroll
-                    for (int q = 0; q < XPL; ++q) {
-                        int col = lane + 32 * q;
-                        x[q] = col < R ? h[q] * Wr[col] : 0.0;
-                    }
-                } else {
-                    int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
-                                        : leaf_index(g, c);
-                    const double *Ur = Uk + t * R;
-#pragma unroll
-                    for (int q = 0; q < XPL; ++q) {
-                        int col = lane + 32 * q;
-                        if (col < R) h[q] *= Ur[col];
-                    }
-                    if (lane == 0) p.samples[(int64_t)k * p.J + i] = (uint64_t)t;
-                }
-            }
+        for (int phase = 0; phase < 2; ++phase) {
+            const T *G = phase == 0 ? (const T *)p.eig_G + k * eig_stride : (const T *)p.gram_G[k];
+            const DGeom &g = phase == 0 ? p.eig : p.gram[k];
+            const double *Uk = p.U[k];
             __syncwarp();
-        }
-        if (p.weights) {
-            double scale = stage_query<RMAX, T>(h, R, xd, xT, lane);
+            stage_query<RMAX, T>(x, R, xd, xT, lane);
             qf.setup(xT, pairs, lane);
-            if (sizeof(T) == 8) {
-                double lev = (double)qf.eval((const T *)(p.M + cm_pinv64_offset(p.N, R)), lane);
-                if (lane == 0) p.weights[i] = (double)R / (lev * (double)p.J);
-            } else {
-                // w = R / (J lev), lev = lev_scaled / scale^2: the quotient in
-                // FP32, the power-of-two rescale as one exact FP64 product
-                float lev_s = (float)qf.eval((const T *)p.pinv32, lane);
-                if (lane == 0) p.weights[i] = (double)(RJ / lev_s) * (scale * scale);
-            }
-        }
-        if (p.h) {
+            T frac;
+            const int64_t c = descend<RMAX>(G, p.S, g, get_draw(p, (int64_t)(phase * p.N + k) * p.J + i),
+                                            qf, lane, frac, (phase == 1 && g.F > 1) ? Uk : nullptr, R);
+            if (phase == 0) {
+                const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)leaf_index(g, c) * R;
 #pragma unroll
-            for (int q = 0; q < XPL; ++q) {
-                int col = lane + 32 * q;
-                if (col < R) p.h[i * R + col] = h[q];
+                for (int q = 0; q < XPL; ++q) {
+                    int col = lane + 32 * q;
+                    x[q] = col < R ? h[q] * Wr[col] : 0.0;
+                }
+            } else {
+                int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
+                                    : leaf_index(g, c);
+                const double *Ur = Uk + t * R;
+#pragma unroll
+                for (int q = 0; q < XPL; ++q) {
+                    int col = lane + 32 * q;
+                    if (col < R) h[q] *= Ur[col];
+                }
+                if (lane == 0) p.samples[(int64_t)k * p.J + i] = (uint64_t)t;
             }
         }
         __syncwarp();
+    }
+    if (p.weights) {
+        double scale = stage_query<RMAX, T>(h, R, xd, xT, lane);
+        qf.setup(xT, pairs, lane);
+        if (sizeof(T) == 8) {
+            double lev = (double)qf.eval((const T *)(p.M + cm_pinv64_offset(p.N, R)), lane);
+            if (lane == 0) p.weights[i] = (double)R / (lev * (double)p.J);
+        } else {
+            // w = R / (J lev), lev = lev_scaled / scale^2: the quotient in
+            // FP32, the power-of-two rescale as one exact FP64 product
+            float lev_s = (float)qf.eval((const T *)p.pinv32, lane);
+            if (lane == 0) p.weights[i] = (double)(RJ / lev_s) * (scale * scale);
+        }
+    }
+    if (p.h) {
+#pragma unroll
+        for (int q = 0; q < XPL; ++q) {
+            int col = lane + 32 * q;
+            if (col < R) p.h[i * R + col] = h[q];
+        }
+    }
+    __syncwarp();
+}
+
+template <int RMAX, typename T>
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DrawWarp<RMAX, T> dw;
+    setup_draw_warp<RMAX, T>(dw, smem_raw, p.R, p.P, p.S);
+    const int warp = threadIdx.x >> 5;
+    for (int64_t i = (int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp; i < p.J;
+         i += (int64_t)gridDim.x * Shape<RMAX>::WARPS)
+        draw_sample<RMAX, T>(p, i, dw);
+}
+
+// Packed draw: the samples of up to FTL_MAX_PACK requests of the same rank
+// and precision in one launch; warp w takes global sample w, which belongs to
+// the request r with cum[r] <= w < cum[r+1].  Each sample runs exactly the
+// code of krp_draw_kernel, so results equal the per-request launches.
+struct MultiDrawParams {
+    int n;
+    int64_t cum[FTL_MAX_PACK + 1];
+    DrawParams req[FTL_MAX_PACK];
+};
+
+template <int RMAX, typename T>
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DrawWarp<RMAX, T> dw;
+    setup_draw_warp<RMAX, T>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+    const int warp = threadIdx.x >> 5;
+    const int64_t total = mp.cum[mp.n];
+    for (int64_t g = (int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp; g < total;
+         g += (int64_t)gridDim.x * Shape<RMAX>::WARPS) {
+        int r = 0;
+        while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
+        draw_sample<RMAX, T>(mp.req[r], g - mp.cum[r], dw);
     }
 }
 
@@ -189,6 +243,17 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
     }
 }
 
+__global__ void philox_fill_dev_kernel(double *out, int64_t n, uint64_t seed, const uint64_t *ctr_dev) {
+    const uint64_t ctr = *ctr_dev;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = philox_uniform(seed, ctr + (uint64_t)i);
+}
+
+__global__ void counter_add_kernel(uint64_t *ctr_dev, uint64_t inc) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *ctr_dev += inc;
+}
+
 __global__ void philox_fill_kernel(double *out, int64_t n, uint64_t seed, uint64_t ctr) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -215,6 +280,23 @@ static int launch_draw(const DrawParams &p, cudaStream_t st) {
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
     krp_draw_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     return check_launch("krp_draw_kernel");
+}
+
+template <int RMAX, typename T>
+static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
+    const int warps = Shape<RMAX>::WARPS;
+    size_t smem = desc_smem<RMAX, T>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(krp_draw_multi_kernel<RMAX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::max<size_t>(smem, 48 * 1024));
+        attr = true;
+    }
+    const int64_t total = mp.cum[mp.n];
+    int64_t blocks = (total + warps - 1) / warps;
+    blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
+    krp_draw_multi_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
+    return check_launch("krp_draw_multi_kernel");
 }
 
 template <int RMAX, typename T>
@@ -301,6 +383,9 @@ extern "C" int ftl_krp_compute_m(const ftl_krp_plan *plan, uint32_t j, void *str
     return computem_launch(plan, jn, (cudaStream_t)stream);
 }
 
+static void fill_draw_params(DrawParams &p, const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
+                             double *weights, const double *draws, uint64_t seed, uint64_t ctr);
+
 extern "C" int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
                               double *weights, const double *draws, uint64_t seed, uint64_t ctr,
                               void *stream) {
@@ -308,6 +393,14 @@ extern "C" int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *sa
     if (rc) return rc;
     FTL_CHECK_ARG(samples != nullptr, "ftl_krp_sample: samples is NULL");
     DrawParams p;
+    fill_draw_params(p, plan, j, samples, h, weights, draws, seed, ctr);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (plan->prec == FTL_PREC_FP64) return dispatch_draw<double>(p, st);
+    return dispatch_draw<float>(p, st);
+}
+
+static void fill_draw_params(DrawParams &p, const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
+                             double *weights, const double *draws, uint64_t seed, uint64_t ctr) {
     p.N = plan->N;
     p.R = plan->R;
     p.P = packed_size(plan->R);
@@ -337,9 +430,39 @@ extern "C" int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *sa
     p.draws = draws;
     p.seed = seed;
     p.ctr = ctr;
+}
+
+extern "C" int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_t *js,
+                                     uint64_t *const *samples, double *const *h, double *const *weights,
+                                     const double *const *draws, const uint64_t *seeds, const uint64_t *ctrs,
+                                     void *stream) {
+    FTL_CHECK_ARG(plans && js && samples && h && weights && seeds && ctrs, "ftl_krp_sample_packed: null array");
+    FTL_CHECK_ARG(n >= 1 && n <= FTL_MAX_PACK, "ftl_krp_sample_packed: n=%d outside [1, %d]", n, FTL_MAX_PACK);
+    MultiDrawParams mp;
+    mp.n = n;
+    mp.cum[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        int rc = validate_plan(plans[i]);
+        if (rc) return rc;
+        FTL_CHECK_ARG(plans[i]->R == plans[0]->R && plans[i]->prec == plans[0]->prec,
+                      "ftl_krp_sample_packed: request %d has R=%d prec=%d, request 0 R=%d prec=%d", i,
+                      plans[i]->R, plans[i]->prec, plans[0]->R, plans[0]->prec);
+        FTL_CHECK_ARG(samples[i] != nullptr, "ftl_krp_sample_packed: samples[%d] is NULL", i);
+        fill_draw_params(mp.req[i], plans[i], js[i], samples[i], h[i], weights[i], draws ? draws[i] : nullptr,
+                         seeds[i], ctrs[i]);
+        mp.cum[i + 1] = mp.cum[i] + plans[i]->J;
+    }
+    for (int i = n; i < FTL_MAX_PACK; ++i) mp.cum[i + 1] = mp.cum[n];
     cudaStream_t st = (cudaStream_t)stream;
-    if (plan->prec == FTL_PREC_FP64) return dispatch_draw<double>(p, st);
-    return dispatch_draw<float>(p, st);
+    const int R = plans[0]->R;
+    if (plans[0]->prec == FTL_PREC_FP64) {
+        if (R <= 32) return launch_multi<32, double>(mp, st);
+        if (R <= 64) return launch_multi<64, double>(mp, st);
+        return launch_multi<128, double>(mp, st);
+    }
+    if (R <= 32) return launch_multi<32, float>(mp, st);
+    if (R <= 64) return launch_multi<64, float>(mp, st);
+    return launch_multi<128, float>(mp, st);
 }
 
 extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
@@ -383,4 +506,14 @@ extern "C" int ftl_philox_uniforms(double *out, int64_t n, uint64_t seed, uint64
     int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 16);
     philox_fill_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(out, n, seed, ctr);
     return check_launch("philox_fill_kernel");
+}
+
+extern "C" int ftl_philox_uniforms_dev(double *out, int64_t n, uint64_t seed, uint64_t *ctr_dev, void *stream) {
+    FTL_CHECK_ARG(out != nullptr && ctr_dev != nullptr && n >= 0, "ftl_philox_uniforms_dev: bad arguments");
+    if (n == 0) return FTL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 16);
+    philox_fill_dev_kernel<<<blocks, 256, 0, st>>>(out, n, seed, ctr_dev);
+    counter_add_kernel<<<1, 32, 0, st>>>(ctr_dev, (uint64_t)n);
+    return check_launch("philox_fill_dev_kernel");
 }

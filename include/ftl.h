@@ -50,6 +50,7 @@ extern "C" {
 
 #define FTL_MAX_MODES 16
 #define FTL_MAX_RANK 128
+#define FTL_MAX_PACK 16  /* requests per packed draw launch */
 
 /* Last error message of the calling thread ("" if none). */
 const char *ftl_last_error(void);
@@ -295,10 +296,28 @@ int ftl_krp_draw_static(int N, int R, int64_t J, int prec, const int64_t *dims,
                         uint64_t *samples_dev, double *h_dev, double *weights_dev,
                         const double *draws_dev, uint64_t seed, uint64_t ctr, void *stream);
 
+/* The descent of n <= FTL_MAX_PACK draws in ONE launch (continuous batching
+ * of concurrent sampling requests).  All plans share R and precision; plan i
+ * must have had ftl_krp_compute_m for js[i] ordered before this call on
+ * `stream`.  Per request the arguments of ftl_krp_sample (draws[i] may be
+ * NULL for the in-kernel Philox stream); each request's results are
+ * identical to its own ftl_krp_sample. */
+int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_t *js,
+                          uint64_t *const *samples_dev, double *const *h_dev,
+                          double *const *weights_dev, const double *const *draws_dev,
+                          const uint64_t *seeds, const uint64_t *ctrs, void *stream);
+
 /* Fill out_dev[0..n) with the uniforms the in-kernel generator uses
  * (Philox4x32-10, key=seed, counter=ctr+i). */
 int ftl_philox_uniforms(double *out_dev, int64_t n, uint64_t seed, uint64_t ctr,
                         void *stream);
+
+/* The same uniforms with the counter read from device memory, which is then
+ * advanced by n: out[i] = Philox4x32-10(seed, *ctr_dev + i); *ctr_dev += n.
+ * Stream-ordered and free of host arguments that change between calls, so a
+ * captured CUDA graph replays with fresh uniforms each time. */
+int ftl_philox_uniforms_dev(double *out_dev, int64_t n, uint64_t seed, uint64_t *ctr_dev,
+                            void *stream);
 
 #ifdef __cplusplus
 }
