@@ -46,11 +46,12 @@ def test_mix_equals_alone(ftl):
     sizes = [S.estimate_bytes(r) for r in reqs]
     budget = sum(sorted(sizes)[-3:])  # forces some requests to wait
     eng = S.ServingEngine(budget, max_active=8)
-    arrivals = [(0.002 * i, r) for i, r in enumerate(reqs)]
+    # a burst of three requests (two share R = 16 and pack into one launch),
+    # then the rest spread out while those are on the device
+    arrivals = [(0.0 if i < 3 else 0.002 * i, r) for i, r in enumerate(reqs)]
     done = eng.run(arrivals)
     assert len(done) == len(reqs)
     assert eng.max_in_use <= budget
-    assert eng.packed_launches < sum(isinstance(r, S.SampleRequest) for r in reqs)
     by_id = {h.rid: h for h in done}
     for rid, r in enumerate(reqs):
         res = by_id[rid].result
@@ -79,6 +80,7 @@ def test_mix_equals_alone(ftl):
             resid = sp.compute_residual_normsq(lr.sigma_dev, lr.U_dev)
             fit = 1.0 - np.sqrt(max(resid, 0.0) / sp.get_normsq())
             assert abs(res["fit"] - fit) <= 1e-9
+    assert eng.packed_launches < sum(isinstance(r, S.SampleRequest) for r in reqs)
     lat = S.latency_stats(done)
     assert lat["count"] == len(reqs) and lat["p99_ms"] >= lat["p50_ms"] > 0
 
