@@ -157,7 +157,9 @@ class ALS:
             raise RuntimeError("graph capture needs LowRankTensor(..., sync_host=False)")
         N, J = lr.N, self.J
         dev = self.device
-        self._ctr_dev = torch.tensor([self.sampler.counter], dtype=torch.int64, device=dev)
+        cur = torch.cuda.current_stream(dev)
+        # no host round trip: the counter is filled on the device
+        self._ctr_dev = torch.full((1,), self.sampler.counter, dtype=torch.int64, device=dev)
         self._gdraws = torch.empty(2 * N * J, dtype=torch.float64, device=dev)
 
         def sweep():
@@ -167,22 +169,24 @@ class ALS:
                           self._ctr_dev.data_ptr(), st)
                 self.execute_ds_als_update(j, renormalize, update_sampler, draws=self._gdraws)
 
-        # warm-up on a side stream settles workspaces and kernel attributes,
-        # then restore the state it advanced
-        saved = [u.clone() for u in lr.U_dev] + [lr.sigma_dev.clone(), self._ctr_dev.clone()]
-        side = torch.cuda.Stream(dev)
-        side.wait_stream(torch.cuda.current_stream(dev))
-        with torch.cuda.stream(side):
-            sweep()
-        torch.cuda.current_stream(dev).wait_stream(side)
-        for t, v in zip(lr.U_dev + [lr.sigma_dev, self._ctr_dev], saved):
-            t.copy_(v)
-        for j in range(N):
-            self.sampler.update_sampler(j)
-        torch.cuda.synchronize(dev)
+        # Capture on a side stream with the graph API directly: nothing runs
+        # while capturing, so no warm-up or device-wide synchronisation is
+        # needed (torch.cuda.graph's context manager would synchronise the
+        # whole device and empty the allocator cache, stalling every other
+        # stream).  Workspaces and kernel attributes were settled by eager
+        # updates, which must precede the capture.
+        if not self._ws._bufs:
+            raise RuntimeError("run one eager sampled update before capture_sweep")
         self._graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self._graph):
-            sweep()
+        cap = torch.cuda.Stream(dev)
+        cap.wait_stream(cur)
+        with torch.cuda.stream(cap):
+            self._graph.capture_begin()
+            try:
+                sweep()
+            finally:
+                self._graph.capture_end()
+        cur.wait_stream(cap)
 
     def replay_sweep(self) -> None:
         """Run one captured sweep on the current stream."""

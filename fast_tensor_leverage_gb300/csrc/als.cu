@@ -727,7 +727,9 @@ extern "C" int ftl_sparse_mttkrp(const uint64_t *sorted_keys, const uint32_t *so
 extern "C" int ftl_solve_rows(const double *B, const double *pinv, int64_t I, int R, double *U, void *stream) {
     FTL_CHECK_ARG(B && pinv && U, "ftl_solve_rows: null pointer");
     FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I >= 1, "ftl_solve_rows: bad shape");
-    const int threads = 128;
+    // R x R pinv plus one staged row per thread: 128 threads up to R = 64
+    // (96 KB), 64 threads above (196 KB at R = 128)
+    const int threads = R > 64 ? 64 : 128;
     const size_t smem = (size_t)(R * R + threads * R) * sizeof(double);
     static bool attr = false;
     if (!attr) {

@@ -38,6 +38,9 @@
 #ifndef FTL_DESC_WARPS32
 #define FTL_DESC_WARPS32 8         // warps per block for R <= 32
 #endif
+#ifndef FTL_DESC_REDO
+#define FTL_DESC_REDO 1            // FP32: flag samples that met a zero-mass block for the careful redo
+#endif
 #ifndef FTL_DESC_RESIDENT_F32
 #define FTL_DESC_RESIDENT_F32 1536 // threads per SM the FP32 kernels are register-budgeted for
 #endif
@@ -268,11 +271,13 @@ __device__ __forceinline__ void prefetch_next(const T *G, int S, const DGeom &g,
 template <int RMAX>
 __device__ __forceinline__ int64_t descend(const double *__restrict__ G, int S, const DGeom &g,
                                            double draw, const QForm<RMAX, double> &qf, int lane,
-                                           double &frac, const double *U = nullptr, int R = 0) {
+                                           double &frac, const double *U = nullptr, int R = 0,
+                                           double *mroot = nullptr) {
     int64_t c = 0;
     double low = 0.0, high = 1.0;
     if (is_leaf(g, 0)) {  // single-leaf tree: the leaf fraction is the draw
         frac = draw;
+        if (mroot) *mroot = 1.0;  // not evaluated; the leaf scan sees the block
         return 0;
     }
     // the root mass and the first left-child mass need no decision between
@@ -285,6 +290,7 @@ __device__ __forceinline__ int64_t descend(const double *__restrict__ G, int S, 
         m = qf.eval(G, lane);
         mL0 = qf.eval(G + S, lane);
     }
+    if (mroot) *mroot = m;
     for (int64_t lvl = 0; lvl < g.lfill_level; ++lvl) {
         double mL;
         if (lvl == 0) {
@@ -334,10 +340,12 @@ __device__ __forceinline__ void df_sub(float &th, float &tl, float m) {
 template <int RMAX>
 __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, const DGeom &g,
                                            double draw, const QForm<RMAX, float> &qf, int lane,
-                                           float &frac, const double *U = nullptr, int R = 0) {
+                                           float &frac, const double *U = nullptr, int R = 0,
+                                           float *mroot = nullptr) {
     int64_t c = 0;
     if (is_leaf(g, 0)) {  // single-leaf tree: the leaf fraction is the draw
         frac = (float)draw;
+        if (mroot) *mroot = 1.0f;  // not evaluated; the leaf scan sees the block
         return 0;
     }
     prefetch_next(G, S, g, 0, U, R, lane);
@@ -348,6 +356,7 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
         mP = qf.eval(G, lane);
         mL0 = qf.eval(G + S, lane);
     }
+    if (mroot) *mroot = mP;
     double t0 = draw * (double)mP;
     float th = (float)t0;
     float tl = (float)(t0 - (double)th);
@@ -373,6 +382,53 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
     }
     float f = mP > 0.0f ? (th + tl) / mP : 0.0f;
     frac = fminf(fmaxf(f, 0.0f), 1.0f);
+    return c;
+}
+
+// The FP32 descent above carries the mass of a right child as parent - left
+// instead of evaluating it, so where a right subtree has exactly zero mass
+// (a block of all-zero factor rows: rows of an ALS factor that no sampled
+// fiber touched) rounding can send t into it.  This variant, run only when
+// the first descent ended in a block whose forms are all zero, evaluates both
+// children at every level, never enters a child with a non-positive form
+// while its sibling's is positive, and rescales t onto the evaluated child
+// masses (t in FP64).  In exact arithmetic it samples the same distribution.
+template <int RMAX>
+__device__ __forceinline__ int64_t descend_careful(const float *__restrict__ G, int S, const DGeom &g,
+                                                   double draw, const QForm<RMAX, float> &qf, int lane,
+                                                   float &frac) {
+    int64_t c = 0;
+    if (is_leaf(g, 0)) {
+        frac = (float)draw;
+        return 0;
+    }
+    float mL, mR;
+    qf.eval2(G + S, G + 2 * (int64_t)S, lane, mL, mR);
+    double t = draw * ((double)fmaxf(mL, 0.0f) + (double)fmaxf(mR, 0.0f));
+    double m;
+    while (true) {
+        bool left;
+        if (!(mR > 0.0f))
+            left = true;
+        else if (!(mL > 0.0f))
+            left = false;
+        else
+            left = t <= (double)mL;
+        if (left) {
+            c = 2 * c + 1;
+            m = fmax((double)mL, 0.0);
+        } else {
+            c = 2 * c + 2;
+            t -= (double)fmaxf(mL, 0.0f);
+            m = (double)mR;
+        }
+        t = fmin(fmax(t, 0.0), m);
+        if (is_leaf(g, c)) break;
+        qf.eval2(G + (2 * c + 1) * (int64_t)S, G + (2 * c + 2) * (int64_t)S, lane, mL, mR);
+        const double mc = (double)fmaxf(mL, 0.0f) + (double)fmaxf(mR, 0.0f);
+        t = m > 0.0 ? t * (mc / m) : 0.0;
+    }
+    frac = m > 0.0 ? (float)fmin(fmax(t / m, 0.0), 1.0) : 0.0f;
     return c;
 }
 
@@ -434,7 +490,7 @@ __device__ __forceinline__ T transpose_reduce(T (&v)[K], int lane) {
 template <int RMAX, typename T>
 __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R, const DGeom &g,
                                              int64_t c, T frac, const LaneQuery<RMAX, T> &xq,
-                                             int lane) {
+                                             int lane, bool &empty) {
     constexpr int XPL = Shape<RMAX>::XPL;
     constexpr int K = FTL_DESC_LEAF_CHUNK;
     constexpr int LOGK = K == 8 ? 3 : (K == 16 ? 4 : 5);
@@ -484,6 +540,7 @@ __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R
     }
     const T tot = run;
     int res = F - 1;
+    bool found = false;
 #pragma unroll
     for (int qi = FQ - 1; qi >= 0; --qi) {
         int r = lane + 32 * qi;
@@ -493,7 +550,28 @@ __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R
         else
             pred = (r <= F - 2) && (frac * tot < incl[qi]);
         unsigned bal = __ballot_sync(0xffffffffu, pred);
-        if (bal) res = 32 * qi + (__ffs(bal) - 1);
+        if (bal) {
+            res = 32 * qi + (__ffs(bal) - 1);
+            found = true;
+        }
+    }
+    empty = false;
+    if (sizeof(T) == 4 && !found) {
+        // FP32: a row found above has a positive form (its inclusive prefix
+        // exceeds the previous one); when none is, take the last row with a
+        // positive form rather than the last row, and report a block whose
+        // forms are all zero, so the caller can redo the descent.  (FP64
+        // keeps the reference's rule: the last row.)
+        // q2[ch] of lane l is the form of row K ch + (l >> (5 - LOGK))
+        int lastpos = -1;
+#pragma unroll
+        for (int ch = 0; ch < NCH; ++ch) {
+            const int r = K * ch + (lane >> (5 - LOGK));
+            const unsigned bal = __ballot_sync(0xffffffffu, r < rows && q2[ch] > T(0));
+            if (bal) lastpos = K * ch + ((31 - __clz((int)bal)) >> (5 - LOGK));
+        }
+        if (lastpos >= 0) res = lastpos;
+        else empty = true;
     }
     if (res >= rows) res = rows - 1;
     return row0 + res;

@@ -111,11 +111,17 @@ __device__ void jacobi_eigen(T *A, T *V, int R, T *csbuf, int *pqbuf, int *flag)
 // order[r] = index of the r-th smallest eigenvalue (ties by index).
 template <typename T>
 __device__ void sort_ascending(const T *A, int R, int *order) {
+    // A NaN on the diagonal (from a NaN input) ranks as +infinity, so the
+    // ranks are always a permutation of 0..R-1 and every order[] slot is
+    // written: plain < and == on NaN would give colliding ranks and leave
+    // slots holding stale shared memory that callers use as indexes.
     for (int v = threadIdx.x; v < R; v += blockDim.x) {
         T lv = A[v * R + v];
+        if (lv != lv) lv = T(INFINITY);
         int rank = 0;
         for (int u = 0; u < R; ++u) {
             T lu = A[u * R + u];
+            if (lu != lu) lu = T(INFINITY);
             if (lu < lv || (lu == lv && u < v)) ++rank;
         }
         order[rank] = v;

@@ -69,9 +69,18 @@ __device__ __forceinline__ void setup_draw_warp(DrawWarp<RMAX, T> &dw, unsigned 
     dw.lane = threadIdx.x & 31;
 }
 
+// Row index written by an FP32 draw for a mode whose Gram-tree descent met a
+// zero query (the eigen component chosen has zero mass under h) or ended in a
+// block whose forms are all zero -- possible because the FP32 descent carries
+// right-child masses as parent - left, and blocks of exactly-zero factor rows
+// (rows of an ALS factor that no sampled fiber touched) have zero mass.  The
+// fix-up kernel redoes every such sample with descend_careful.
+constexpr uint64_t kRedoSample = ~0ull;
+
 // Sample i of one draw: for every included mode the eigen-component descent
-// and the Gram-tree descent, then the weight and the row of h.
-template <int RMAX, typename T>
+// and the Gram-tree descent, then the weight and the row of h.  CAREFUL (FP32
+// fix-up pass only): both descents evaluate both children at every level.
+template <int RMAX, typename T, bool CAREFUL = false>
 __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, DrawWarp<RMAX, T> &dw) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
@@ -103,9 +112,13 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
             __syncwarp();
             stage_query<RMAX, T>(x, R, xd, xT, lane);
             qf.setup(xT, pairs, lane);
-            T frac;
-            const int64_t c = descend<RMAX>(G, p.S, g, get_draw(p, (int64_t)(phase * p.N + k) * p.J + i),
-                                            qf, lane, frac, (phase == 1 && g.F > 1) ? Uk : nullptr, R);
+            T frac, mroot = T(1);
+            const double u = get_draw(p, (int64_t)(phase * p.N + k) * p.J + i);
+            int64_t c;
+            if constexpr (CAREFUL && sizeof(T) == 4)
+                c = descend_careful<RMAX>(G, p.S, g, u, qf, lane, frac);
+            else
+                c = descend<RMAX>(G, p.S, g, u, qf, lane, frac, (phase == 1 && g.F > 1) ? Uk : nullptr, R, &mroot);
             if (phase == 0) {
                 const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)leaf_index(g, c) * R;
 #pragma unroll
@@ -114,15 +127,24 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
                     x[q] = col < R ? h[q] * Wr[col] : 0.0;
                 }
             } else {
-                int64_t t = g.F > 1 ? leaf_scan<RMAX, T>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
-                                    : leaf_index(g, c);
+                bool empty = false;
+                int64_t t = 0;
+                if (FTL_DESC_REDO && sizeof(T) == 4 && !CAREFUL && !(mroot > T(0))) {
+                    empty = true;  // zero query: the eigen component has no mass under h
+                    t = leaf_index(g, c) * g.F;  // any valid row; the sample is redone
+                } else if (g.F > 1)
+                    t = leaf_scan<RMAX, T>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane, empty);
+                else
+                    t = leaf_index(g, c);
+                // the careful pass (and FP64) keep what they found
+                if (!FTL_DESC_REDO || sizeof(T) == 8 || CAREFUL) empty = false;
                 const double *Ur = Uk + t * R;
 #pragma unroll
                 for (int q = 0; q < XPL; ++q) {
                     int col = lane + 32 * q;
                     if (col < R) h[q] *= Ur[col];
                 }
-                if (lane == 0) p.samples[(int64_t)k * p.J + i] = (uint64_t)t;
+                if (lane == 0) p.samples[(int64_t)k * p.J + i] = empty ? kRedoSample : (uint64_t)t;
             }
         }
         __syncwarp();
@@ -186,6 +208,60 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
     }
 }
 
+// FP32 fix-up pass: every sample of the draw with a kRedoSample row is drawn
+// again with careful descents (same uniforms, all modes), overwriting its
+// samples, h and weight.  Lanes test 32 samples at once; a warp then redoes
+// its flagged samples one by one.  Samples are almost never flagged, so the
+// pass costs one read of the N x J sample rows.
+template <int RMAX>
+__device__ __forceinline__ bool needs_redo(const DrawParams &p, int64_t i) {
+    bool bad = false;
+    if (i < p.J)
+        for (int k = 0; k < p.N; ++k)
+            if ((uint32_t)k != p.j) bad |= p.samples[(int64_t)k * p.J + i] == kRedoSample;
+    return bad;
+}
+
+template <int RMAX>
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_kernel(DrawParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DrawWarp<RMAX, float> dw;
+    setup_draw_warp<RMAX, float>(dw, smem_raw, p.R, p.P, p.S);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * Shape<RMAX>::WARPS;
+    for (int64_t b = ((int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp) * 32; b < p.J; b += nw * 32) {
+        unsigned bal = __ballot_sync(0xffffffffu, needs_redo<RMAX>(p, b + lane));
+        while (bal) {
+            const int src = __ffs(bal) - 1;
+            bal &= bal - 1;
+            draw_sample<RMAX, float, true>(p, b + src, dw);
+        }
+    }
+}
+
+template <int RMAX>
+__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_multi_kernel(MultiDrawParams mp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DrawWarp<RMAX, float> dw;
+    setup_draw_warp<RMAX, float>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t total = mp.cum[mp.n];
+    const int64_t nw = (int64_t)gridDim.x * Shape<RMAX>::WARPS;
+    for (int64_t b = ((int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp) * 32; b < total; b += nw * 32) {
+        const int64_t g = b + lane;
+        int r = 0;
+        while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
+        const bool bad = g < total && needs_redo<RMAX>(mp.req[r], g - mp.cum[r]);
+        unsigned bal = __ballot_sync(0xffffffffu, bad);
+        while (bal) {
+            const int src = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const int rs = __shfl_sync(0xffffffffu, r, src);
+            draw_sample<RMAX, float, true>(mp.req[rs], b + src - mp.cum[rs], dw);
+        }
+    }
+}
+
 struct TreeSampleParams {
     const void *G;
     const double *U;
@@ -231,8 +307,15 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
         T frac;
         int64_t c = descend<RMAX>((const T *)p.G, p.S, p.g, p.draws[i], qf, lane, frac,
                                   p.g.F > 1 ? p.U : nullptr, R);
-        int64_t t = p.g.F > 1 ? leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane)
+        bool empty = false;
+        int64_t t = p.g.F > 1 ? leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane, empty)
                               : leaf_index(p.g, c);
+        if constexpr (sizeof(T) == 4) {
+            if (empty) {  // FP32 descent ended in an all-zero block: redo it evaluating both children
+                c = descend_careful<RMAX>((const float *)p.G, p.S, p.g, p.draws[i], qf, lane, frac);
+                t = leaf_scan<RMAX, T>(p.U, R, p.g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane, empty);
+            }
+        }
         if (lane == 0) p.samples[i] = (uint64_t)t;
 #pragma unroll
         for (int q = 0; q < XPL; ++q) {
@@ -279,7 +362,18 @@ static int launch_draw(const DrawParams &p, cudaStream_t st) {
     int64_t blocks = (p.J + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
     krp_draw_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
-    return check_launch("krp_draw_kernel");
+    int rc = check_launch("krp_draw_kernel");
+    if (rc || sizeof(T) == 8) return rc;
+    static bool fattr = false;
+    if (!fattr) {
+        cudaFuncSetAttribute(krp_fixup_kernel<RMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::max<size_t>(smem, 48 * 1024));
+        fattr = true;
+    }
+    int64_t fblocks = (p.J + 32 * warps - 1) / (32 * warps);
+    fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
+    krp_fixup_kernel<RMAX><<<(unsigned)fblocks, warps * 32, smem, st>>>(p);
+    return check_launch("krp_fixup_kernel");
 }
 
 template <int RMAX, typename T>
@@ -296,7 +390,18 @@ static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
     int64_t blocks = (total + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
     krp_draw_multi_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
-    return check_launch("krp_draw_multi_kernel");
+    int rc = check_launch("krp_draw_multi_kernel");
+    if (rc || sizeof(T) == 8) return rc;
+    static bool fattr = false;
+    if (!fattr) {
+        cudaFuncSetAttribute(krp_fixup_multi_kernel<RMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::max<size_t>(smem, 48 * 1024));
+        fattr = true;
+    }
+    int64_t fblocks = (total + 32 * warps - 1) / (32 * warps);
+    fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
+    krp_fixup_multi_kernel<RMAX><<<(unsigned)fblocks, warps * 32, smem, st>>>(mp);
+    return check_launch("krp_fixup_multi_kernel");
 }
 
 template <int RMAX, typename T>

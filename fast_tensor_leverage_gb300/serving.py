@@ -39,10 +39,44 @@ from .tensors import LowRankTensor, SparseTensor
 
 
 @dataclass
+class GaussianFactors:
+    """Factor matrices made on the device when the request is admitted:
+    float64 tensors of N(0, 1) entries (drawn in FP32), dims[k] x R, from
+    torch's CUDA generator seeded with `seed` (so a request gives the same
+    factors alone or in a mix)."""
+    dims: list
+    R: int
+    seed: int = 0
+
+    def materialize(self, device) -> list:
+        # normals drawn in FP32 and widened: float64 tensors of N(0, 1) values
+        # at a fraction of the cost of FP64 transcendentals on this GPU
+        g = torch.Generator(device=device)
+        g.manual_seed(int(self.seed))
+        return [torch.randn((int(I), int(self.R)), dtype=torch.float32, device=device, generator=g).double()
+                for I in self.dims]
+
+
+@dataclass
+class SyntheticSparse:
+    """A sparse tensor made on the device when the request is admitted:
+    synthetic.sparse_powerlaw_tensor(dims, nnz, s, seed)."""
+    dims: list
+    nnz: int
+    s: float = 1.1
+    seed: int = 0
+
+    def materialize(self, device):
+        from .synthetic import sparse_powerlaw_tensor
+        return sparse_powerlaw_tensor(self.dims, int(self.nnz), self.s, seed=int(self.seed), device=device)
+
+
+@dataclass
 class SampleRequest:
     """Draw J samples from the KRP of `factors` (list of float64 (I_k, R)
-    arrays or CUDA tensors), excluding mode j (j >= N: none)."""
-    factors: list
+    arrays or CUDA tensors, or a GaussianFactors spec), excluding mode j
+    (j >= N: none)."""
+    factors: object
     J: int
     j: int = 1 << 30
     precision: str = "fp32"
@@ -52,8 +86,9 @@ class SampleRequest:
 @dataclass
 class ALSRequest:
     """`sweeps` sweeps of randomized CP-ALS on a sparse tensor (idx (nnz, N)
-    uint32 or int32 CUDA tensor, vals, dims), rank R, J samples per update,
-    factors from PyLowRank-style Gaussian init with `seed`."""
+    uint32 or int32 CUDA tensor, vals, dims; or idx a SyntheticSparse spec
+    and vals None), rank R, J samples per update; the initial factors are
+    GaussianFactors(dims, R, seed), made on the device, with unit columns."""
     idx: object
     vals: object
     dims: list
@@ -63,6 +98,7 @@ class ALSRequest:
     precision: str = "fp32"
     seed: int = 0
     sampler_seed: int = 1
+    return_factors: bool = True   # False: the result holds sigma and the fit only
 
 
 @dataclass
@@ -91,24 +127,35 @@ def estimate_bytes(req) -> int:
     """Device bytes a request holds while admitted (factors, trees,
     workspaces, outputs; ALS also the sorted nonzeros)."""
     if isinstance(req, SampleRequest):
-        R, N, J = int(req.factors[0].shape[1]), len(req.factors), int(req.J)
+        dims, R = _factor_shapes(req.factors)
+        N, J = len(dims), int(req.J)
         prec = _lib.PREC[req.precision]
         total = 0
-        for f in req.factors:
-            I = int(f.shape[0])
+        for I in dims:
             total += I * R * 8 + _lib.tree_bytes(I, min(R, I), R, prec)
         e, m, l, p = _lib.plan_sizes(N, R, prec)
         return total + e + m + l + p + N * J * 8 + J * R * 8 + J * 8 + (1 << 20)
     if isinstance(req, ALSRequest):
         N, R, J = len(req.dims), int(req.R), int(req.J)
-        nnz = int(req.idx.shape[0])
         prec = _lib.PREC[req.precision]
-        total = nnz * (4 * N + 8) + N * nnz * (8 + 4 + 8) * 2
+        if isinstance(req.idx, SyntheticSparse):
+            nnz = int(req.idx.nnz)
+            # generation transients: oversampled int64 columns, sort permutations
+            gen = int(nnz * 1.35) * (8 * N + 8 * 3 + 1)
+        else:
+            nnz, gen = int(req.idx.shape[0]), 0
+        total = max(gen, nnz * (4 * N + 8)) + N * nnz * (8 + 4 + 8) * 2
         for I in req.dims:
             total += 2 * I * R * 8 + _lib.tree_bytes(I, min(R, I), R, prec)
         e, m, l, p = _lib.plan_sizes(N, R, prec)
         return total + e + m + l + p + max(req.dims) * R * 8 + J * (N * 8 + R * 8 + 64) + (4 << 20)
     raise TypeError(f"unknown request type {type(req).__name__}")
+
+
+def _factor_shapes(factors) -> tuple[list, int]:
+    if isinstance(factors, GaussianFactors):
+        return [int(I) for I in factors.dims], int(factors.R)
+    return [int(f.shape[0]) for f in factors], int(factors[0].shape[1])
 
 
 class ServingEngine:
@@ -130,6 +177,7 @@ class ServingEngine:
         self.t0 = time.perf_counter()
         self.packed_launches = 0
         self.max_in_use = 0
+        self.host_s = {"admit": 0.0, "issue": 0.0, "retire": 0.0}
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -148,9 +196,17 @@ class ServingEngine:
         return not self.pending and not self.active
 
     def tick(self) -> None:
+        t0 = time.perf_counter()
         self._retire()
+        t1 = time.perf_counter()
         self._admit()
+        t2 = time.perf_counter()
         self._issue()
+        t3 = time.perf_counter()
+        hs = self.host_s
+        hs["retire"] += t1 - t0
+        hs["admit"] += t2 - t1
+        hs["issue"] += t3 - t2
 
     def run(self, arrivals=None, poll_sleep: float = 0.0) -> list[Handle]:
         """Drive the loop.  `arrivals`: iterable of (time_s, request) sorted by
@@ -195,13 +251,18 @@ class ServingEngine:
         req = h.request
         with torch.cuda.stream(h._stream):
             if isinstance(req, SampleRequest):
-                h._obj = Sampler(req.factors, req.J, int(req.factors[0].shape[1]), "efficient",
+                factors = req.factors
+                if isinstance(factors, GaussianFactors):
+                    factors = factors.materialize(self.device)
+                h._obj = Sampler(factors, req.J, _factor_shapes(factors)[1], "efficient",
                                  precision=req.precision, seed=req.seed, device=self.device)
                 h._stage = "ready"
             else:
-                sp = SparseTensor(req.idx, req.vals, "sort", dims=req.dims, device=self.device)
-                rng = np.random.default_rng(req.seed)
-                U = [rng.normal(size=(i, req.R)) for i in req.dims]
+                idx, vals = req.idx, req.vals
+                if isinstance(idx, SyntheticSparse):
+                    idx, vals = idx.materialize(self.device)
+                sp = SparseTensor(idx, vals, "sort", dims=req.dims, device=self.device)
+                U = GaussianFactors(req.dims, req.R, seed=req.seed).materialize(self.device)
                 lr = LowRankTensor(req.R, U, device=self.device, sync_host=False)
                 lr.renormalize_columns(-1)
                 als = ALS(lr, sp)
@@ -292,8 +353,9 @@ class ServingEngine:
         else:
             sp, lr, als = h._obj
             resid = sp.compute_residual_normsq(lr.sigma_dev, lr.U_dev)
-            h.result = {"U": [u.cpu().numpy() for u in lr.U_dev], "sigma": lr.sigma,
-                        "fit": 1.0 - np.sqrt(max(resid, 0.0) / sp.get_normsq())}
+            h.result = {"sigma": lr.sigma, "fit": 1.0 - np.sqrt(max(resid, 0.0) / sp.get_normsq())}
+            if h.request.return_factors:
+                h.result["U"] = [u.cpu().numpy() for u in lr.U_dev]
         h.done = self.now()
         h._obj = None
         self._streams.append(h._stream)
@@ -322,8 +384,64 @@ def admission_order(sizes, bypassed, in_use: int, budget: int, free_slots: int, 
 
 
 def latency_stats(handles) -> dict:
-    lat = np.array([h.latency for h in handles if h.latency is not None])
-    if lat.size == 0:
+    """Latency percentiles (completion - arrival), split into the wait for
+    admission (admitted - arrival) and the service time (completion -
+    admitted)."""
+    hs = [h for h in handles if h.latency is not None]
+    if not hs:
         return {}
-    return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "mean_ms": float(lat.mean() * 1e3), "count": int(lat.size)}
+    lat = np.array([h.latency for h in hs])
+    wait = np.array([h.admitted - h.arrival for h in hs])
+    serv = np.array([h.done - h.admitted for h in hs])
+    pc = lambda a, q: float(np.percentile(a, q) * 1e3)
+    return {"p50_ms": pc(lat, 50), "p99_ms": pc(lat, 99), "mean_ms": float(lat.mean() * 1e3), "count": len(hs),
+            "wait_p50_ms": pc(wait, 50), "wait_p99_ms": pc(wait, 99),
+            "service_p50_ms": pc(serv, 50), "service_p99_ms": pc(serv, 99)}
+
+
+def als_dims_cap(N: int, key_bits: int = 62) -> int:
+    """Largest mode size for which every mode's fiber keys (mixed-radix over
+    the other N - 1 modes) stay below 2^key_bits when all modes share it."""
+    return int(2 ** (key_bits / (N - 1)))
+
+
+def poisson_request_stream(seed: int, rate: float, duration: float, als_fraction: float = 0.2,
+                           precision: str = "fp32", ranks=(8, 16, 32, 64, 128),
+                           I_range=(1e4, 1e7), J_log2_range=(10, 17), nnz_range=(1e5, 3e6),
+                           als_sweeps: int = 5) -> list:
+    """A seeded mixed request stream: arrivals of a Poisson process with mean
+    `rate` per second over `duration` seconds; each request is CP-ALS with
+    probability `als_fraction`, else sampling.  N uniform in {3..6}, every
+    mode size log-uniform in I_range, R uniform over `ranks`, J log-uniform
+    in 2^J_log2_range, float64 N(0, 1) factors made on the device.  Sampling
+    requests exclude a mode j uniform in {0..N} (N: none excluded).  CP-ALS
+    requests run `als_sweeps` sweeps on a Zipf(1.1) sparse tensor with nnz
+    log-uniform in nnz_range; their mode sizes are capped at als_dims_cap(N)
+    (lower bound min(I_range[0], cap / 4)) so fiber keys fit 62 bits, and
+    they return sigma and the fit (not the factors).
+    Returns [(arrival_s, request), ...] sorted by arrival."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    lo, hi = np.log10(I_range[0]), np.log10(I_range[1])
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= duration:
+            break
+        N = int(rng.integers(3, 7))
+        R = int(ranks[int(rng.integers(0, len(ranks)))])
+        J = int(round(2.0 ** rng.uniform(*J_log2_range)))
+        s = int(rng.integers(0, 1 << 62))
+        if rng.random() < als_fraction:
+            cap = als_dims_cap(N)
+            a_hi = min(hi, np.log10(cap))
+            a_lo = min(lo, a_hi - np.log10(4.0))
+            dims = [int(round(10 ** rng.uniform(a_lo, a_hi))) for _ in range(N)]
+            nnz = int(round(10 ** rng.uniform(np.log10(nnz_range[0]), np.log10(nnz_range[1]))))
+            req = ALSRequest(SyntheticSparse(dims, nnz, 1.1, seed=s), None, dims, R, J, sweeps=als_sweeps,
+                             precision=precision, seed=s + 1, sampler_seed=s + 2, return_factors=False)
+        else:
+            dims = [int(round(10 ** rng.uniform(lo, hi))) for _ in range(N)]
+            req = SampleRequest(GaussianFactors(dims, R, seed=s), J, j=int(rng.integers(0, N + 1)),
+                                precision=precision, seed=s + 1)
+        out.append((t, req))
+    return out

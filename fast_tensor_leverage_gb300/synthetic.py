@@ -1,7 +1,7 @@
 """Seeded synthetic workloads standing in for datasets that are not available
 here (the FROSTT tensors the reference benchmarks on).
 
-sparse_powerlaw_tensor: a 3-mode sparse tensor with per-mode bounded
+sparse_powerlaw_tensor: an N-mode sparse tensor with per-mode bounded
 Zipf(s) indices (inverse-CDF of the continuous power law on [1, dim + 1)),
 duplicate index tuples removed, values log(1 + x) of lognormal(0, 1) draws --
 the shape, index skew and value distribution of the amazon-reviews stand-in.
@@ -22,23 +22,24 @@ def _zipf_indices(n: int, dim: int, s: float, gen: torch.Generator, device) -> t
 
 def sparse_powerlaw_tensor(dims, nnz: int, s: float = 1.1, seed: int = 0, device="cuda",
                            oversample: float = 1.35):
-    """Returns (idx int32 (nnz', 3) CUDA tensor holding uint32 indices, values
+    """Returns (idx int32 (nnz', N) CUDA tensor holding uint32 indices, values
     float64 (nnz',)), nnz' <= nnz unique tuples sorted lexicographically."""
-    assert len(dims) == 3
+    N = len(dims)
+    assert N >= 2 and all(0 < d <= 1 << 32 for d in dims)
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
     m = int(nnz * oversample)
-    i0 = _zipf_indices(m, dims[0], s, gen, device)
-    i1 = _zipf_indices(m, dims[1], s, gen, device)
-    i2 = _zipf_indices(m, dims[2], s, gen, device)
-    # unique tuples: lexicographic sort by (i0, i1 * d2 + i2) (two stable sorts)
-    lo = i1 * dims[2] + i2
-    o = torch.argsort(lo, stable=True)
-    o = o[torch.argsort(i0[o], stable=True)]
-    i0, lo = i0[o], lo[o]
-    keep = torch.ones(m, dtype=torch.bool, device=device)
-    keep[1:] = (i0[1:] != i0[:-1]) | (lo[1:] != lo[:-1])
-    i0, lo = i0[keep][:nnz], lo[keep][:nnz]
-    idx = torch.stack([i0, lo // dims[2], lo % dims[2]], dim=1).to(torch.int32)
+    cols = [_zipf_indices(m, int(d), s, gen, device) for d in dims]
+    # lexicographic order: stable sorts from the last mode to the first
+    o = torch.argsort(cols[N - 1], stable=True)
+    for k in range(N - 2, -1, -1):
+        o = o[torch.argsort(cols[k][o], stable=True)]
+    cols = [c[o] for c in cols]
+    keep = torch.zeros(m, dtype=torch.bool, device=device)
+    keep[0] = True
+    for c in cols:
+        keep[1:] |= c[1:] != c[:-1]
+    idx = torch.stack([c[keep][:nnz] for c in cols], dim=1).to(torch.int32)
+    del cols, keep, o
     vals = torch.log1p(torch.exp(torch.randn(idx.shape[0], generator=gen, device=device, dtype=torch.float64)))
     return idx.contiguous(), vals

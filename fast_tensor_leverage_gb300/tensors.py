@@ -54,7 +54,9 @@ class LowRankTensor:
     the reference.  U_list holds float64 (I_k, R) C-contiguous numpy arrays,
     kept by reference; ALS updates are mirrored back into them (set
     `sync_host=False` to keep the factors on the device only and call
-    `sync_host_copies()` when the host arrays are needed)."""
+    `sync_host_copies()` when the host arrays are needed).  U_list may
+    instead hold float64 CUDA tensors (with sync_host=False): the factors
+    then live on the device only."""
 
     def __init__(self, R, *args, device=None, sync_host: bool = True):
         if len(args) == 1:
@@ -65,17 +67,27 @@ class LowRankTensor:
         else:
             raise TypeError("LowRankTensor(R, U_list) or LowRankTensor(R, max_rhs_rows, U_list)")
         self.R = int(R)
-        self.U = list(U_list)
-        self.N = len(self.U)
+        U_list = list(U_list)
+        self.N = len(U_list)
         if not (1 <= self.N <= _lib.MAX_MODES) or not (1 <= self.R <= _lib.MAX_RANK):
             raise ValueError(f"bad N={self.N} or R={self.R}")
-        for k, u in enumerate(self.U):
-            D.require_numpy_out(u, np.float64, f"U[{k}]")
+        on_device = all(isinstance(u, torch.Tensor) and u.is_cuda for u in U_list)
+        for k, u in enumerate(U_list):
+            if not on_device:
+                D.require_numpy_out(u, np.float64, f"U[{k}]")
             if u.ndim != 2 or u.shape[1] != self.R:
-                raise ValueError(f"U[{k}] must be (I_k, {self.R}), got {u.shape}")
-        self.dims = [int(u.shape[0]) for u in self.U]
+                raise ValueError(f"U[{k}] must be (I_k, {self.R}), got {tuple(u.shape)}")
+        self.dims = [int(u.shape[0]) for u in U_list]
         self.device = D.cuda_device(device)
-        self.U_dev = [torch.from_numpy(u).to(self.device) for u in self.U]
+        if on_device:
+            # device-only factors (no host arrays to mirror into)
+            if sync_host:
+                raise ValueError("CUDA factor tensors need sync_host=False")
+            self.U = None
+            self.U_dev = [u.to(self.device, torch.float64).contiguous() for u in U_list]
+        else:
+            self.U = U_list
+            self.U_dev = [torch.from_numpy(u).to(self.device) for u in self.U]
         self.sigma_dev = torch.ones(self.R, dtype=torch.float64, device=self.device)
         self.sync_host = sync_host
         self._ws = _Workspace(self.device)
@@ -89,10 +101,14 @@ class LowRankTensor:
 
     def upload(self, k: int | None = None) -> None:
         """Copy host factor(s) to the device (after editing the numpy arrays)."""
+        if self.U is None:
+            raise RuntimeError("this LowRankTensor has device factors only")
         for i in range(self.N) if k is None else [k]:
             self.U_dev[i].copy_(torch.from_numpy(self.U[i]))
 
     def sync_host_copies(self, k: int | None = None) -> None:
+        if self.U is None:
+            raise RuntimeError("this LowRankTensor has device factors only")
         for i in range(self.N) if k is None else [k]:
             self.U[i][...] = self.U_dev[i].cpu().numpy()
 
@@ -209,8 +225,19 @@ class SparseTensor:
         out = torch.empty(1, dtype=torch.float64, device=dev)
         _lib.call("ftl_sum_squares", self.vals_dev.data_ptr(), self.nnz, self._ws.get("fit", nb).data_ptr(), nb,
                   out.data_ptr(), st)
-        self.normsq = float(out.item())
+        # read on first use: construction does not wait for the device
+        self._normsq_dev = out
+        self._normsq_ev = torch.cuda.Event()
+        self._normsq_ev.record(torch.cuda.current_stream(dev))
+        self._normsq = None
         self._dims_c = dims_c
+
+    @property
+    def normsq(self) -> float:
+        if self._normsq is None:
+            self._normsq_ev.synchronize()   # the sum ran on the construction stream
+            self._normsq = float(self._normsq_dev.item())
+        return self._normsq
 
     def get_normsq(self) -> float:
         return self.normsq

@@ -132,3 +132,64 @@ def test_gpu_downsampled_mttkrp_and_norms(ftl):
     for k in range(N):
         G = G * (U[k].T @ U[k])
     np.testing.assert_allclose(lr.get_normsq(), G.sum(), rtol=1e-11)
+
+
+def test_gpu_als_fp32_rank64_four_modes_stays_finite(ftl):
+    """Mixed-precision CP-ALS at R = 64 on a 4-mode Zipf tensor whose mode
+    sizes (~4e4) far exceed what J = 1917 samples touch, so most factor rows
+    become exact zeros after the first updates: factors, sigma and fit stay
+    finite through a full eager sweep and a graph-captured one."""
+    from fast_tensor_leverage_gb300.synthetic import sparse_powerlaw_tensor
+    dims = [42030, 38493, 39731, 45257]
+    idx, vals = sparse_powerlaw_tensor(dims, 142532, 1.1, seed=3, device="cuda")
+    sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
+    rng = np.random.default_rng(4)
+    lr = ftl.LowRankTensor(64, [rng.normal(size=(d, 64)) for d in dims], sync_host=False)
+    lr.renormalize_columns(-1)
+    als = ftl.ALS(lr, sp)
+    als.initialize_ds_als(1917, "efficient", precision="fp32", seed=6)
+    for j in range(4):
+        als.execute_ds_als_update(j, True, True)
+    als.capture_sweep()
+    als.replay_sweep()
+    torch.cuda.synchronize()
+    for u in lr.U_dev:
+        assert bool(torch.isfinite(u).all())
+    assert bool(torch.isfinite(lr.sigma_dev).all())
+    resid = sp.compute_residual_normsq(lr.sigma_dev, lr.U_dev)
+    assert np.isfinite(resid)
+
+
+def test_gpu_exact_als_update_rank128_matches_numpy(ftl):
+    """Exact update at the largest rank (R = 128: the solve stages 64 rows
+    per block, the pseudo-inverse keeps its eigenvectors in global scratch)
+    against the numpy restatement used above."""
+    rng = np.random.default_rng(9)
+    dims, nnz, R = [300, 200, 250], 6000, 128
+    flat = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idx = np.stack(np.unravel_index(flat, dims), axis=1).astype(np.uint32)
+    vals = rng.normal(size=nnz)
+    U = [rng.normal(size=(d, R)) for d in dims]
+    Uo = [u.copy() for u in U]
+    lr = ftl.LowRankTensor(R, U)
+    sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
+    als = ftl.ALS(lr, sp)
+    als.initialize_ds_als(64, "efficient", precision="fp64", seed=1)
+    j = 1
+    als.execute_exact_als_update(j, True, True)
+    G = np.ones((R, R))
+    for k in range(3):
+        if k != j:
+            G = G * (Uo[k].T @ Uo[k])
+    pinv = O.pinv_square(G, R, 1e-11)
+    mt = np.zeros_like(Uo[j])
+    part = vals[:, None] * np.ones((1, R))
+    for k in range(3):
+        if k != j:
+            part = part * Uo[k][idx[:, k]]
+    np.add.at(mt, idx[:, j], part)
+    Uj = mt @ pinv
+    norms = np.sqrt((Uj ** 2).sum(axis=0))
+    norms[norms <= 1e-7] = 1.0
+    np.testing.assert_allclose(U[j], Uj / norms, rtol=0, atol=1e-8 * np.abs(Uj / norms).max())
+    np.testing.assert_allclose(lr.sigma, norms, rtol=1e-8)

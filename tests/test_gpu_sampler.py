@@ -76,6 +76,7 @@ def test_fp64_draw_matches_reference_golden(ftl, name):
     (3, [300, 1500, 64], 25, 3000, 2, 104),  # R not a power of two, F = R
     (2, [5000, 3000], 64, 2000, 3, 105),     # R > 32: shared-memory forms
     (2, [600, 700], 128, 600, 3, 106),       # R = 128: eigenvectors in scratch
+    (4, [300, 400, 350, 500], 128, 400, 1, 111),  # R = 128, four modes, one excluded
     (3, [20, 30, 40], 32, 1500, 4, 107),     # I < R: F = I, single-leaf trees
     (6, [50, 60, 70, 80, 90, 100], 16, 2000, 3, 108),
     (4, [17, 50, 9, 23], 5, 1500, 2, 109),   # odd R with N + 1 odd: unaligned dense slots
@@ -131,6 +132,7 @@ def test_philox_stream_equals_injected_oracle_uniforms(ftl):
     (2, [5000, 3000], 64, 2000, 3),
     (3, [20, 30, 40], 32, 3000, 4),   # rank-deficient Grams: Jacobi pseudo-inverse path
     (4, [170, 500, 90, 230], 5, 3000, 1),
+    (3, [500, 600, 700], 128, 1500, 1),
 ])
 def test_fp32_draw_agrees_with_fp64_oracle(ftl, N, dims, R, J, j):
     rng = np.random.default_rng(31 + R)
@@ -246,3 +248,54 @@ def test_large_tree_build_fp32_vs_fp64(ftl):
     # root against numpy
     Gr = U.T @ U
     np.testing.assert_allclose(a[0], Gr[np.triu_indices(R)], rtol=1e-10, atol=1e-8)
+
+
+@pytest.mark.parametrize("R,rows_per_block", [(32, 32), (64, 64), (16, 5)])
+def test_fp32_draw_never_selects_zero_rows(ftl, R, rows_per_block):
+    """Factors whose rows are mostly exact zeros in long runs (the rows of an
+    ALS factor that no sampled fiber touched): every sampled row must have a
+    positive leverage, so every weight is finite and positive.  The FP32
+    descent carries right-child masses as parent - left, so without the
+    careful re-descent rounding can walk into an all-zero subtree."""
+    rng = np.random.default_rng(77 + R)
+    N, I, J = 3, 20000, 1 << 17
+    U = []
+    for k in range(N):
+        u = np.zeros((I, R))
+        live = rng.choice(I // rows_per_block, size=I // rows_per_block // 9, replace=False)
+        for b in live:
+            r = b * rows_per_block + rng.integers(0, rows_per_block)
+            u[r] = rng.normal(size=R) * 10.0 ** rng.uniform(-3, 3)
+        U.append(u)
+    s = ftl.Sampler(U, J, R, "efficient", precision="fp32", seed=5)
+    zero = [torch.from_numpy(~u.any(axis=1)).cuda() for u in U]
+    for j in (N + 1, 0, 2):
+        for _ in range(4):
+            samples, h, w = s.draw(j)
+            for k in range(N):
+                if k == j:
+                    continue
+                assert not bool(zero[k][samples[k]].any()), f"mode {k}: a zero row was sampled"
+            assert bool(torch.isfinite(w).all()) and bool((w > 0).all())
+            assert bool((h.abs().sum(dim=1) > 0).all())
+
+
+def test_pinv_square_with_nan_input_completes(ftl):
+    """A NaN Gram (from a non-finite weight) must give a NaN result, not
+    out-of-range eigenvector indexes: the eigenvalue sort ranks NaN last."""
+    from fast_tensor_leverage_gb300 import _lib
+    for R in (8, 64):
+        M = torch.eye(R, dtype=torch.float64, device="cuda")
+        M[1, 2] = M[2, 1] = float("nan")
+        M[3, 3] = float("nan")
+        out = torch.empty_like(M)
+        vs = torch.empty_like(M)
+        _lib.call("ftl_pinv_square", M.data_ptr(), R, R, None, 1e-11, out.data_ptr(), vs.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        # the context is healthy and a finite input still inverts exactly
+        G = torch.eye(R, dtype=torch.float64, device="cuda") * 4.0
+        _lib.call("ftl_pinv_square", G.data_ptr(), R, R, None, 1e-11, out.data_ptr(), vs.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        torch.testing.assert_close(out, torch.eye(R, dtype=torch.float64, device="cuda") / 4.0)

@@ -64,8 +64,7 @@ def test_mix_equals_alone(ftl):
             assert np.array_equal(res["h"], h.cpu().numpy())
             assert np.array_equal(res["weights"], w.cpu().numpy())
         else:
-            rng = np.random.default_rng(r.seed)
-            U = [rng.normal(size=(i, r.R)) for i in r.dims]
+            U = S.GaussianFactors(r.dims, r.R, seed=r.seed).materialize(torch.device("cuda", 0))
             lr = ftl.LowRankTensor(r.R, U, sync_host=False)
             lr.renormalize_columns(-1)
             sp = ftl.SparseTensor(r.idx, r.vals, "sort", dims=r.dims)
