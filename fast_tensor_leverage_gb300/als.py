@@ -45,6 +45,7 @@ class ALS:
         self.device = cp_decomp.device
         self.sampler: Sampler | None = None
         self.J = None
+        self._eager_done = False
         self._ws = _Workspace(self.device)
         self.last_update = {}
 
@@ -72,6 +73,15 @@ class ALS:
         self._vscr = torch.empty((R, R), dtype=torch.float64, device=dev)
         self._mttkrp = torch.empty(max(lr.dims) * R, dtype=torch.float64, device=dev)
         self._dims_c = (ctypes.c_int64 * lr.N)(*lr.dims)
+        # every buffer an update uses is sized here, so updates (and captured
+        # sweeps) allocate nothing
+        self._ws.get("dedup", _lib.ws_bytes("dedup", J))
+        self._ws.get("gram", _lib.ws_bytes("gram", R))
+        lr._ws.get("colnorm", _lib.ws_bytes("colnorm", R))
+        if getattr(lr, "_norms", None) is None:
+            lr._norms = torch.empty((lr.N, R), dtype=torch.float64, device=dev)
+        self._ctr_dev = torch.zeros(1, dtype=torch.int64, device=dev)
+        self._gdraws = torch.empty(2 * lr.N * J, dtype=torch.float64, device=dev)
 
     # ------------------------------------------------------------------ updates
     def execute_ds_als_update(self, j: int, renormalize: bool = True, update_sampler: bool = True,
@@ -82,6 +92,7 @@ class ALS:
         N, R, J = lr.N, lr.R, self.J
         j = int(j)
         st = D.stream_ptr(self.device)
+        self._eager_done = True
         samples, h, w = self.sampler.draw(j, draws)
         # fiber keys of the samples on modes != j (samples are N x J)
         _lib.call("ftl_fiber_keys", samples.data_ptr(), 1, J, 1, J, N, self._dims_c, j, self._keys.data_ptr(), st)
@@ -159,8 +170,7 @@ class ALS:
         dev = self.device
         cur = torch.cuda.current_stream(dev)
         # no host round trip: the counter is filled on the device
-        self._ctr_dev = torch.full((1,), self.sampler.counter, dtype=torch.int64, device=dev)
-        self._gdraws = torch.empty(2 * N * J, dtype=torch.float64, device=dev)
+        self._ctr_dev.fill_(self.sampler.counter)
 
         def sweep():
             st = D.stream_ptr(dev)
@@ -175,7 +185,7 @@ class ALS:
         # whole device and empty the allocator cache, stalling every other
         # stream).  Workspaces and kernel attributes were settled by eager
         # updates, which must precede the capture.
-        if not self._ws._bufs:
+        if not self._eager_done:
             raise RuntimeError("run one eager sampled update before capture_sweep")
         self._graph = torch.cuda.CUDAGraph()
         cap = torch.cuda.Stream(dev)

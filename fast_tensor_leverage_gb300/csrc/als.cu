@@ -170,12 +170,15 @@ static int64_t table_size_for(int64_t J) {
 
 // partial[b][e] = sum over this block's rows u of s_u * h_a h_b, e = packed
 // (a, b); rows u < *n_rows (or n_rows_host), h row = lhs[row(u)], s_u =
-// (w ? w[row(u)] : 1) * (cnt ? cnt[u] : 1).
+// (w ? w[row(u)] : 1) * (cnt ? cnt[u] : 1).  All-zero rows are skipped (they
+// add exact zeros): most rows of a sampled-ALS factor are zero, and this is
+// FP64 arithmetic at a low issue rate.
 __global__ void gram_partial_kernel(const double *__restrict__ lhs, const int32_t *__restrict__ rowidx,
                                     const double *__restrict__ w, const int32_t *__restrict__ cnt,
                                     const int64_t *__restrict__ n_rows_dev, int64_t n_rows_host, int R,
                                     double *__restrict__ partial) {
-    extern __shared__ double hs[];  // 32 rows x R, then P scale slots
+    extern __shared__ double hs[];  // 32 rows x R, then 32 scale slots
+    __shared__ int nz[32];          // row has a nonzero entry
     const int P = packed_size(R);
     const int64_t n = n_rows_dev ? *n_rows_dev : n_rows_host;
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
@@ -202,11 +205,15 @@ __global__ void gram_partial_kernel(const double *__restrict__ lhs, const int32_
         for (int64_t u0 = r0; u0 < r1; u0 += 32) {
             const int m = (int)min((int64_t)32, r1 - u0);
             __syncthreads();
+            if (threadIdx.x < 32) nz[threadIdx.x] = 0;
+            __syncthreads();
             for (int e = threadIdx.x; e < m * R; e += blockDim.x) {
                 int uu = e / R, col = e - uu * R;
                 int64_t u = u0 + uu;
                 int64_t row = rowidx ? rowidx[u] : u;
-                hs[e] = lhs[row * R + col];
+                const double v = lhs[row * R + col];
+                hs[e] = v;
+                if (v != 0.0) nz[uu] = 1;
             }
             for (int uu = threadIdx.x; uu < m; uu += blockDim.x) {
                 int64_t u = u0 + uu;
@@ -215,6 +222,7 @@ __global__ void gram_partial_kernel(const double *__restrict__ lhs, const int32_
             }
             __syncthreads();
             for (int uu = 0; uu < m; ++uu) {
+                if (!nz[uu]) continue;
                 const double *hr = hs + uu * R;
                 const double su = sc[uu];
 #pragma unroll

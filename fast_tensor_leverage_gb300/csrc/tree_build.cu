@@ -159,11 +159,15 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     int LB = std::max(1, 256 / tiles);
     while (LB > 1 && (size_t)LB * blk_bytes > 112u * 1024u) --LB;
     size_t smem = (size_t)LB * blk_bytes;
-    if (smem > 48 * 1024) {
-        if (smem > 227 * 1024)
-            return fail(FTL_E_UNSUPPORTED, "tree_build: leaf block of %lld x %d needs %zu B of shared memory",
-                        (long long)F, R, smem);
-        cudaFuncSetAttribute(leaf_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 227 * 1024)
+        return fail(FTL_E_UNSUPPORTED, "tree_build: leaf block of %lld x %d needs %zu B of shared memory",
+                    (long long)F, R, smem);
+    // once per process (one device): changing a kernel's attributes on every
+    // call can wait for launches of it that are still running
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(leaf_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
     }
     int64_t nbatch = (geom.leaf_count + LB - 1) / LB;
     int grid = (int)std::min<int64_t>(nbatch, (int64_t)sm_count() * 8);

@@ -6,11 +6,16 @@ Requests of uneven N, I, R and J arrive over time.  The engine:
     (first fit: a request that does not fit yet does not block smaller ones
     behind it for more than `max_bypass` admissions);
   * keeps each admitted request's factors, partition trees and workspaces
-    resident on the device until it completes, and gives it its own CUDA
-    stream, so admitted requests overlap on the device;
+    resident on the device until it completes; admission work (factor and
+    tree construction, computeM, sparse sorting) runs on one set-up stream,
+    so freed memory is reused by later requests;
   * packs the descents of concurrent sampling requests that share rank and
     precision into ONE launch (ftl_krp_sample_packed, up to FTL_MAX_PACK
-    requests), after each request's computeM on its own stream;
+    requests) on a draw stream, after their set-up;
+  * gives each CP-ALS request its own stream for its sweeps, so requests
+    overlap on the device;
+  * copies results to pinned host memory on the stream that made them, so
+    completion needs no host synchronisation;
   * runs CP-ALS requests sweep by sweep, each sweep replaying a captured CUDA
     graph after the first (eager) sweep;
   * records arrival, admission and completion times; latency = completion -
@@ -117,6 +122,7 @@ class Handle:
     _sweeps_done: int = 0
     _stage: str = "pending"
     _bypassed: int = 0
+    _host: list = None
 
     @property
     def latency(self) -> float | None:
@@ -160,7 +166,7 @@ def _factor_shapes(factors) -> tuple[list, int]:
 
 class ServingEngine:
     def __init__(self, hbm_budget_bytes: int, max_active: int = 32, device=None, pack: bool = True,
-                 max_bypass: int = 8, graph_als: bool = True):
+                 max_bypass: int = 8, graph_als: bool = True, reserve: bool = False):
         self.device = D.cuda_device(device)
         self.budget = int(hbm_budget_bytes)
         self.max_active = int(max_active)
@@ -173,11 +179,26 @@ class ServingEngine:
         self.in_use = 0
         self._next = 0
         self._pack_stream = torch.cuda.Stream(self.device)
+        # Admission work (factors, trees, computeM, sparse sorting, ALS
+        # buffers) runs on one stream: torch's caching allocator keys free
+        # blocks by the allocating stream, so memory freed by finished
+        # requests is reused by the next ones instead of stranding in
+        # per-stream caches.
+        self._setup_stream = torch.cuda.Stream(self.device)
         self._streams = [torch.cuda.Stream(self.device) for _ in range(self.max_active)]
+        if reserve:
+            # Map the whole budget once: later requests split cached blocks
+            # instead of asking the driver for memory while other requests
+            # run (large device allocations can synchronise the device).
+            with torch.cuda.stream(self._setup_stream):
+                block = torch.empty(self.budget, dtype=torch.uint8, device=self.device)
+                del block
         self.t0 = time.perf_counter()
         self.packed_launches = 0
         self.max_in_use = 0
         self.host_s = {"admit": 0.0, "issue": 0.0, "retire": 0.0}
+        self.start_s: list[float] = []   # host seconds spent admitting each request
+        self.start_log: list[tuple] = []  # (seconds, kind, N, R, max I, bytes) per admission
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -241,21 +262,22 @@ class ServingEngine:
         self.max_in_use = max(self.max_in_use, self.in_use)
 
     def _start(self, h: Handle) -> None:
+        t_start = time.perf_counter()
         h.admitted = self.now()
         self.in_use += h.bytes
-        # streams come from a fixed pool, so the caching allocator can reuse
-        # the blocks of finished requests
-        if not self._streams:
-            self._streams.append(torch.cuda.Stream(self.device))
-        h._stream = self._streams.pop()
         req = h.request
-        with torch.cuda.stream(h._stream):
+        st = self._setup_stream
+        with torch.cuda.stream(st):
             if isinstance(req, SampleRequest):
                 factors = req.factors
                 if isinstance(factors, GaussianFactors):
                     factors = factors.materialize(self.device)
-                h._obj = Sampler(factors, req.J, _factor_shapes(factors)[1], "efficient",
-                                 precision=req.precision, seed=req.seed, device=self.device)
+                s = Sampler(factors, req.J, _factor_shapes(factors)[1], "efficient",
+                            precision=req.precision, seed=req.seed, device=self.device)
+                _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), min(req.j, 1 << 31), int(st.cuda_stream))
+                h._obj = s
+                h._event = torch.cuda.Event()
+                h._event.record(st)
                 h._stage = "ready"
             else:
                 idx, vals = req.idx, req.vals
@@ -269,7 +291,21 @@ class ServingEngine:
                 als.initialize_ds_als(req.J, "efficient", precision=req.precision, seed=req.sampler_seed)
                 h._obj = (sp, lr, als)
                 h._stage = "als"
+        if h._stage == "als":
+            # sweeps run on the request's own stream, after its set-up
+            if not self._streams:
+                self._streams.append(torch.cuda.Stream(self.device))
+            h._stream = self._streams.pop()
+            h._stream.wait_stream(st)
         self.active.append(h)
+        dt = time.perf_counter() - t_start
+        self.start_s.append(dt)
+        if isinstance(req, SampleRequest):
+            dims, R = _factor_shapes(req.factors)
+        else:
+            dims, R = req.dims, req.R
+        self.start_log.append((dt, "sample" if isinstance(req, SampleRequest) else "als", len(dims), R,
+                               max(dims), h.bytes))
 
     def _issue(self) -> None:
         ready = [h for h in self.active if h._stage == "ready"]
@@ -287,17 +323,9 @@ class ServingEngine:
         for (R, prec), hs in groups.items():
             for i in range(0, len(hs), 16 if self.pack else 1):
                 chunk = hs[i:i + (16 if self.pack else 1)]
-                ev = []
-                for h in chunk:
-                    s: Sampler = h._obj
-                    j = h.request.j
-                    _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), j, int(h._stream.cuda_stream))
-                    e = torch.cuda.Event()
-                    e.record(h._stream)
-                    ev.append(e)
                 ps = self._pack_stream
-                for e in ev:
-                    ps.wait_event(e)
+                for h in chunk:
+                    ps.wait_event(h._event)   # set-up and computeM done
                 n = len(chunk)
                 plans = (ctypes.POINTER(_lib.KRPPlan) * n)(*[ctypes.pointer(h._obj._plan) for h in chunk])
                 js = (ctypes.c_uint32 * n)(*[min(h.request.j, 1 << 31) for h in chunk])
@@ -309,6 +337,15 @@ class ServingEngine:
                 _lib.call("ftl_krp_sample_packed", plans, n, js, smp, hh, ww, None, seeds, ctrs,
                           int(ps.cuda_stream))
                 self.packed_launches += 1
+                # results to pinned host buffers on the same stream: completion
+                # needs no host synchronisation
+                with torch.cuda.stream(ps):
+                    for h in chunk:
+                        s: Sampler = h._obj
+                        srcs = (s.samples_dev, s.h_dev, s.weights_dev)
+                        h._host = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in srcs]
+                        for dst, src in zip(h._host, srcs):
+                            dst.copy_(src, non_blocking=True)
                 done = torch.cuda.Event()
                 done.record(ps)
                 for h in chunk:
@@ -330,11 +367,20 @@ class ServingEngine:
             else:
                 als.replay_sweep()
             h._sweeps_done += 1
+            if h._sweeps_done >= req.sweeps:
+                # the fit terms and the result copies follow the last sweep on
+                # this stream
+                terms = sp.residual_terms_async(lr.sigma_dev, lr.U_dev)
+                srcs = [terms, lr.sigma_dev, sp._normsq_dev]
+                if req.return_factors:
+                    srcs += list(lr.U_dev)
+                h._host = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in srcs]
+                for dst, src in zip(h._host, srcs):
+                    dst.copy_(src, non_blocking=True)
+                h._stage = "running"
             e = torch.cuda.Event()
             e.record(h._stream)
             h._event = e
-        if h._sweeps_done >= req.sweeps:
-            h._stage = "running"
 
     def _retire(self) -> None:
         keep = []
@@ -346,19 +392,21 @@ class ServingEngine:
         self.active = keep
 
     def _finish(self, h: Handle) -> None:
+        # h._event covers the result copies: the pinned buffers are complete
         if isinstance(h.request, SampleRequest):
-            s: Sampler = h._obj
-            h.result = {"samples": s.samples_dev.cpu().numpy().view(np.uint64),
-                        "h": s.h_dev.cpu().numpy(), "weights": s.weights_dev.cpu().numpy()}
+            samples, hh, w = (t.numpy() for t in h._host)
+            h.result = {"samples": samples.view(np.uint64), "h": hh, "weights": w}
         else:
-            sp, lr, als = h._obj
-            resid = sp.compute_residual_normsq(lr.sigma_dev, lr.U_dev)
-            h.result = {"sigma": lr.sigma, "fit": 1.0 - np.sqrt(max(resid, 0.0) / sp.get_normsq())}
+            terms, sigma, normsq = (t.numpy() for t in h._host[:3])
+            resid = float(terms[0] + terms[1])
+            h.result = {"sigma": sigma, "fit": 1.0 - np.sqrt(max(resid, 0.0) / float(normsq[0]))}
             if h.request.return_factors:
-                h.result["U"] = [u.cpu().numpy() for u in lr.U_dev]
+                h.result["U"] = [t.numpy() for t in h._host[3:]]
+        h._host = None
         h.done = self.now()
         h._obj = None
-        self._streams.append(h._stream)
+        if h._stream is not None:
+            self._streams.append(h._stream)
         h._stream = None
         h._event = None
         self.in_use -= h.bytes

@@ -135,7 +135,9 @@ class LowRankTensor:
         nb = _lib.ws_bytes("colnorm", self.R)
         w = self._ws.get("colnorm", nb)
         modes = range(self.N) if j == -1 else [j]
-        norms = torch.empty((self.N, self.R), dtype=torch.float64, device=self.device)
+        if getattr(self, "_norms", None) is None:
+            self._norms = torch.empty((self.N, self.R), dtype=torch.float64, device=self.device)
+        norms = self._norms
         for i in modes:
             _lib.call("ftl_renormalize_columns", self.U_dev[i].data_ptr(), self.dims[i], self.R,
                       norms[i].data_ptr(), w.data_ptr(), nb, 1, st)
@@ -255,6 +257,12 @@ class SparseTensor:
         """||X - [[sigma; U]]||^2 = sum_nnz (v^2 - 2 v model) + ||model||^2
         (sparse_tensor.hpp:117-119, sort_lookup.hpp:134-197).  U_list items
         may be numpy arrays or CUDA tensors (a LowRankTensor's U_dev)."""
+        t = self.residual_terms_async(sigma, U_list).cpu().numpy()
+        return float(t[0] + t[1])
+
+    def residual_terms_async(self, sigma, U_list) -> torch.Tensor:
+        """The two terms of compute_residual_normsq as a (2,) CUDA tensor,
+        enqueued on the current stream without waiting for them."""
         st = D.stream_ptr(self.device)
         if isinstance(sigma, torch.Tensor):
             sig = sigma.to(self.device, torch.float64).contiguous()
@@ -269,8 +277,7 @@ class SparseTensor:
         G = [factor_gram(u, self._ws, st) for u in Ud]
         _lib.call("ftl_gram_hadamard", _ptrs(G), self.N, R, -1, sig.data_ptr(), sig.data_ptr(), None,
                   terms[1:2].data_ptr(), st)
-        t = terms.cpu().numpy()
-        return float(t[0] + t[1])
+        return terms
 
     def execute_downsampled_mttkrp_py(self, samples, lhs, j: int, result) -> None:
         """result (I_j x R) = sum over the rows i of samples (J x N uint64) of
