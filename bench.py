@@ -148,13 +148,15 @@ def make_factors_device(N, I, R, seed, device):
     return U
 
 
-def algorithmic_bytes(samples, dims, R, J, N, j, prec_bytes):
+def algorithmic_bytes(samples, dims, R, J, N, j, prec_bytes, shadow=False):
     """Bytes one descent launch must move at minimum (each distinct node or
     leaf block read once): per included mode, distinct Gram-tree nodes read
     (root + left child of every internal node on a sampled path) x P x s_G,
-    distinct leaf blocks x rows x R x 8 (FP64 factor rows of the leaf scan),
-    the whole eigen tree (2R-1) x P x s_G and its R x R FP64 row table; plus
-    the outputs (samples N x J x 8, h J x R x 8, weights J x 8)."""
+    distinct leaf blocks x rows x R x 8 (FP64 factor rows of the leaf scan;
+    x 4 when the scan reads the FP32 factor copies, plus distinct sampled
+    rows x R x 8 for the FP64 rows that update h), the whole eigen tree
+    (2R-1) x P x s_G and its R x R FP64 row table; plus the outputs
+    (samples N x J x 8, h J x R x 8, weights J x 8)."""
     import torch
     from fast_tensor_leverage_gb300 import _lib
     P = R * (R + 1) // 2
@@ -179,7 +181,11 @@ def algorithmic_bytes(samples, dims, R, J, N, j, prec_bytes):
             reads.append(torch.unique(2 * parent + 1))
             cur = torch.unique(parent)
         n_nodes = int(torch.unique(torch.cat(reads)).numel())
-        total += n_nodes * P * prec_bytes + int(leaves.numel()) * F * R * 8
+        if shadow:
+            total += n_nodes * P * prec_bytes + int(leaves.numel()) * F * R * 4
+            total += int(torch.unique(rows).numel()) * R * 8
+        else:
+            total += n_nodes * P * prec_bytes + int(leaves.numel()) * F * R * 8
         total += (2 * R - 1) * P * prec_bytes + R * R * 8
     n_inc = sum(1 for k in range(N) if k != j)
     total += n_inc * J * 8 + J * R * 8 + J * 8
@@ -274,7 +280,7 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize(dev)
     kernel_ms = e0.elapsed_time(e1) / ksteps
     prec_bytes = 4 if args.precision == "fp32" else 8
-    alg = algorithmic_bytes(s.samples_dev, s.dims, R, J, N, j, prec_bytes)
+    alg = algorithmic_bytes(s.samples_dev, s.dims, R, J, N, j, prec_bytes, shadow=s.U32 is not None)
     peak, peak_kind = measured_peak()
     achieved = alg / (kernel_ms / 1e3) / 1e9
     traffic = read_traffic(args.precision)

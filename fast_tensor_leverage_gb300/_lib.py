@@ -54,6 +54,7 @@ class KRPPlan(ctypes.Structure):
         ("M", ctypes.c_void_p),
         ("lambda_", ctypes.c_void_p),
         ("pinv32", ctypes.c_void_p),
+        ("U32", ctypes.c_void_p * MAX_MODES),
     ]
 
 
@@ -69,6 +70,7 @@ _SZP = ctypes.POINTER(ctypes.c_size_t)
 SIGNATURES = {
     "ftl_last_error": ([], ctypes.c_char_p),
     "ftl_abi_version": ([], _INT),
+    "ftl_factor_shadow": ([_P, _I64, _P, _P], _INT),
     "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),
     "ftl_tree_bytes": ([_I64, _I64, _INT, _INT, _SZP], _INT),
     "ftl_tree_build": ([_P, _I64, _INT, _I64, _INT, _P, _P], _INT),

@@ -487,8 +487,8 @@ __device__ __forceinline__ T transpose_reduce(T (&v)[K], int lane) {
 // transpose-reduce.  xq holds the warp's query in the compute type.  A
 // selection past the last row of a partial block (only reachable when frac
 // rounds to >= 1) is clamped to that last row.
-template <int RMAX, typename T>
-__device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R, const DGeom &g,
+template <int RMAX, typename T, typename UT = double>
+__device__ __forceinline__ int64_t leaf_scan(const UT *__restrict__ U, int R, const DGeom &g,
                                              int64_t c, T frac, const LaneQuery<RMAX, T> &xq,
                                              int lane, bool &empty) {
     constexpr int XPL = Shape<RMAX>::XPL;
@@ -508,7 +508,7 @@ __device__ __forceinline__ int64_t leaf_scan(const double *__restrict__ U, int R
             const int r = K * ch + rr;
             T acc = T(0);
             if (r < rows) {
-                const double *u = U + (row0 + r) * (int64_t)R;
+                const UT *u = U + (row0 + r) * (int64_t)R;
 #pragma unroll
                 for (int q = 0; q < XPL; ++q) {
                     const int col = lane + 32 * q;

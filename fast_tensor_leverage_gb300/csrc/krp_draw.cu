@@ -25,6 +25,7 @@ struct DrawParams {
     DGeom gram[FTL_MAX_MODES];
     DGeom eig;
     const double *U[FTL_MAX_MODES];
+    const float *U32[FTL_MAX_MODES];  // FP32 copies of U for the leaf scans (S32 kernels)
     const void *gram_G[FTL_MAX_MODES];
     const void *eig_G;
     const double *M;
@@ -80,7 +81,7 @@ constexpr uint64_t kRedoSample = ~0ull;
 // Sample i of one draw: for every included mode the eigen-component descent
 // and the Gram-tree descent, then the weight and the row of h.  CAREFUL (FP32
 // fix-up pass only): both descents evaluate both children at every level.
-template <int RMAX, typename T, bool CAREFUL = false>
+template <int RMAX, typename T, bool CAREFUL = false, bool S32 = false>
 __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, DrawWarp<RMAX, T> &dw) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
@@ -133,7 +134,10 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
                     empty = true;  // zero query: the eigen component has no mass under h
                     t = leaf_index(g, c) * g.F;  // any valid row; the sample is redone
                 } else if (g.F > 1)
-                    t = leaf_scan<RMAX, T>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane, empty);
+                    t = S32 ? leaf_scan<RMAX, T, float>(p.U32[k], R, g, c, frac, lane_query<RMAX, T>(xT, R, lane),
+                                                        lane, empty)
+                            : leaf_scan<RMAX, T, double>(Uk, R, g, c, frac, lane_query<RMAX, T>(xT, R, lane), lane,
+                                                         empty);
                 else
                     t = leaf_index(g, c);
                 // the careful pass (and FP64) keep what they found
@@ -172,7 +176,7 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
     __syncwarp();
 }
 
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool S32>
 __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, T> dw;
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
     const int warp = threadIdx.x >> 5;
     for (int64_t i = (int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp; i < p.J;
          i += (int64_t)gridDim.x * Shape<RMAX>::WARPS)
-        draw_sample<RMAX, T>(p, i, dw);
+        draw_sample<RMAX, T, false, S32>(p, i, dw);
 }
 
 // Packed draw: the samples of up to FTL_MAX_PACK requests of the same rank
@@ -193,7 +197,7 @@ struct MultiDrawParams {
     DrawParams req[FTL_MAX_PACK];
 };
 
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool S32>
 __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, T> dw;
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
          g += (int64_t)gridDim.x * Shape<RMAX>::WARPS) {
         int r = 0;
         while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
-        draw_sample<RMAX, T>(mp.req[r], g - mp.cum[r], dw);
+        draw_sample<RMAX, T, false, S32>(mp.req[r], g - mp.cum[r], dw);
     }
 }
 
@@ -222,7 +226,7 @@ __device__ __forceinline__ bool needs_redo(const DrawParams &p, int64_t i) {
     return bad;
 }
 
-template <int RMAX>
+template <int RMAX, bool S32>
 __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_kernel(DrawParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, float> dw;
@@ -234,12 +238,12 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_kernel(Draw
         while (bal) {
             const int src = __ffs(bal) - 1;
             bal &= bal - 1;
-            draw_sample<RMAX, float, true>(p, b + src, dw);
+            draw_sample<RMAX, float, true, S32>(p, b + src, dw);
         }
     }
 }
 
-template <int RMAX>
+template <int RMAX, bool S32>
 __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_multi_kernel(MultiDrawParams mp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, float> dw;
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_multi_kerne
             const int src = __ffs(bal) - 1;
             bal &= bal - 1;
             const int rs = __shfl_sync(0xffffffffu, r, src);
-            draw_sample<RMAX, float, true>(mp.req[rs], b + src - mp.cum[rs], dw);
+            draw_sample<RMAX, float, true, S32>(mp.req[rs], b + src - mp.cum[rs], dw);
         }
     }
 }
@@ -349,58 +353,58 @@ static size_t desc_smem() {
            (size_t)Shape<RMAX>::WARPS * WarpSlot<RMAX, T>::bytes;
 }
 
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool S32>
 static int launch_draw(const DrawParams &p, cudaStream_t st) {
     const int warps = Shape<RMAX>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(krp_draw_kernel<RMAX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(krp_draw_kernel<RMAX, T, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max<size_t>(smem, 48 * 1024));
         attr = true;
     }
     int64_t blocks = (p.J + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
+    krp_draw_kernel<RMAX, T, S32><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     int rc = check_launch("krp_draw_kernel");
     if (rc || sizeof(T) == 8) return rc;
     static bool fattr = false;
     if (!fattr) {
-        cudaFuncSetAttribute(krp_fixup_kernel<RMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(krp_fixup_kernel<RMAX, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max<size_t>(smem, 48 * 1024));
         fattr = true;
     }
     int64_t fblocks = (p.J + 32 * warps - 1) / (32 * warps);
     fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
-    krp_fixup_kernel<RMAX><<<(unsigned)fblocks, warps * 32, smem, st>>>(p);
+    krp_fixup_kernel<RMAX, S32><<<(unsigned)fblocks, warps * 32, smem, st>>>(p);
     return check_launch("krp_fixup_kernel");
 }
 
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool S32>
 static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
     const int warps = Shape<RMAX>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(krp_draw_multi_kernel<RMAX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(krp_draw_multi_kernel<RMAX, T, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max<size_t>(smem, 48 * 1024));
         attr = true;
     }
     const int64_t total = mp.cum[mp.n];
     int64_t blocks = (total + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_multi_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
+    krp_draw_multi_kernel<RMAX, T, S32><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
     int rc = check_launch("krp_draw_multi_kernel");
     if (rc || sizeof(T) == 8) return rc;
     static bool fattr = false;
     if (!fattr) {
-        cudaFuncSetAttribute(krp_fixup_multi_kernel<RMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(krp_fixup_multi_kernel<RMAX, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max<size_t>(smem, 48 * 1024));
         fattr = true;
     }
     int64_t fblocks = (total + 32 * warps - 1) / (32 * warps);
     fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
-    krp_fixup_multi_kernel<RMAX><<<(unsigned)fblocks, warps * 32, smem, st>>>(mp);
+    krp_fixup_multi_kernel<RMAX, S32><<<(unsigned)fblocks, warps * 32, smem, st>>>(mp);
     return check_launch("krp_fixup_multi_kernel");
 }
 
@@ -420,11 +424,25 @@ static int launch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
     return check_launch("tree_sample_kernel");
 }
 
+// FP32 draws read the leaf blocks from the FP32 factor copies when every
+// sampled mode has one (the values are the same FP32 roundings the scan
+// would make of the FP64 rows, so the results are identical).
+static bool shadows_ready(const DrawParams &p) {
+    for (int k = 0; k < p.N; ++k)
+        if ((uint32_t)k != p.j && p.U32[k] == nullptr) return false;
+    return true;
+}
+
 template <typename T>
 static int dispatch_draw(const DrawParams &p, cudaStream_t st) {
-    if (p.R <= 32) return launch_draw<32, T>(p, st);
-    if (p.R <= 64) return launch_draw<64, T>(p, st);
-    return launch_draw<128, T>(p, st);
+    if (sizeof(T) == 4 && shadows_ready(p)) {
+        if (p.R <= 32) return launch_draw<32, T, true>(p, st);
+        if (p.R <= 64) return launch_draw<64, T, true>(p, st);
+        return launch_draw<128, T, true>(p, st);
+    }
+    if (p.R <= 32) return launch_draw<32, T, false>(p, st);
+    if (p.R <= 64) return launch_draw<64, T, false>(p, st);
+    return launch_draw<128, T, false>(p, st);
 }
 
 // The register/shared-memory shapes are chosen by max(R, F): a lane handles
@@ -517,10 +535,12 @@ static void fill_draw_params(DrawParams &p, const ftl_krp_plan *plan, uint32_t j
             Geom g = make_geom(plan->dims[k], std::min<int64_t>(plan->R, plan->dims[k]));
             p.gram[k] = to_dgeom(g);
             p.U[k] = plan->U[k];
+            p.U32[k] = plan->prec == FTL_PREC_FP32 ? plan->U32[k] : nullptr;
             p.gram_G[k] = plan->gram_G[k];
             p.offset[k] = ((uint32_t)(k + 1) == p.j) ? k + 2 : k + 1;
         } else {
             p.U[k] = nullptr;
+            p.U32[k] = nullptr;
             p.gram_G[k] = nullptr;
             p.offset[k] = 0;
         }
@@ -561,13 +581,20 @@ extern "C" int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, co
     cudaStream_t st = (cudaStream_t)stream;
     const int R = plans[0]->R;
     if (plans[0]->prec == FTL_PREC_FP64) {
-        if (R <= 32) return launch_multi<32, double>(mp, st);
-        if (R <= 64) return launch_multi<64, double>(mp, st);
-        return launch_multi<128, double>(mp, st);
+        if (R <= 32) return launch_multi<32, double, false>(mp, st);
+        if (R <= 64) return launch_multi<64, double, false>(mp, st);
+        return launch_multi<128, double, false>(mp, st);
     }
-    if (R <= 32) return launch_multi<32, float>(mp, st);
-    if (R <= 64) return launch_multi<64, float>(mp, st);
-    return launch_multi<128, float>(mp, st);
+    bool s32 = true;
+    for (int i = 0; i < n; ++i) s32 = s32 && shadows_ready(mp.req[i]);
+    if (s32) {
+        if (R <= 32) return launch_multi<32, float, true>(mp, st);
+        if (R <= 64) return launch_multi<64, float, true>(mp, st);
+        return launch_multi<128, float, true>(mp, st);
+    }
+    if (R <= 32) return launch_multi<32, float, false>(mp, st);
+    if (R <= 64) return launch_multi<64, float, false>(mp, st);
+    return launch_multi<128, float, false>(mp, st);
 }
 
 extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
@@ -621,4 +648,19 @@ extern "C" int ftl_philox_uniforms_dev(double *out, int64_t n, uint64_t seed, ui
     philox_fill_dev_kernel<<<blocks, 256, 0, st>>>(out, n, seed, ctr_dev);
     counter_add_kernel<<<1, 32, 0, st>>>(ctr_dev, (uint64_t)n);
     return check_launch("philox_fill_dev_kernel");
+}
+
+namespace ftl {
+__global__ void shadow_kernel(const double *__restrict__ U, int64_t n, float *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)U[i];
+}
+}  // namespace ftl
+
+extern "C" int ftl_factor_shadow(const double *U, int64_t count, float *out, void *stream) {
+    FTL_CHECK_ARG(U && out && count >= 0, "ftl_factor_shadow: bad arguments");
+    if (count == 0) return FTL_OK;
+    int blocks = (int)std::min<int64_t>((count + 255) / 256, (int64_t)num_sms() * 16);
+    shadow_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(U, count, out);
+    return check_launch("shadow_kernel");
 }

@@ -83,7 +83,7 @@ extern "C" int ftl_krp_draw_static(int N, int R, int64_t J, int prec, const int6
     void *base = nullptr;
     rc = scratch_address(&base);
     if (rc) return rc;
-    ftl_krp_plan plan;
+    ftl_krp_plan plan = {};
     plan.N = N;
     plan.R = R;
     plan.J = J;

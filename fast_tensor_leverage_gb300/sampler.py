@@ -22,7 +22,7 @@ from . import _lib
 
 class Sampler:
     def __init__(self, U, J: int, R: int, type: str = "efficient", *, precision: str = "fp64",
-                 seed: int | None = None, device=None):
+                 seed: int | None = None, device=None, factor_shadows: bool = True):
         if type != "efficient":
             raise ValueError(
                 f"Unsupported argument {type!r} passed for sampler construction "
@@ -49,6 +49,10 @@ class Sampler:
         dev = self.device
         self.U = [f.to(dev, torch.float64).contiguous() if isinstance(f, torch.Tensor)
                   else torch.from_numpy(f).to(dev) for f in factors]
+        # FP32 mode: FP32 copies of the factors for the leaf scans (half the
+        # leaf-block bytes, same results); refreshed with each tree
+        self.U32 = ([torch.empty((n, R), dtype=torch.float32, device=dev) for n in self.dims]
+                    if precision == "fp32" and factor_shadows else None)
         self.trees = []
         for k in range(N):
             nb = _lib.tree_bytes(self.dims[k], self.F[k], R, self._prec)
@@ -85,6 +89,7 @@ class Sampler:
         for k in range(self.N):
             p.dims[k] = self.dims[k]
             p.U[k] = self.U[k].data_ptr()
+            p.U32[k] = self.U32[k].data_ptr() if self.U32 is not None else None
             p.gram_G[k] = self.trees[k].data_ptr()
         p.eig_G = self.eig_G.data_ptr()
         p.M = self.M.data_ptr()
@@ -100,6 +105,9 @@ class Sampler:
         (EfficientKRPSampler::update_sampler, efficient_krp_sampler.hpp:73-75)."""
         _lib.call("ftl_tree_build", self.U[j].data_ptr(), self.dims[j], self.R, self.F[j],
                   self._prec, self.trees[j].data_ptr(), self._stream(stream))
+        if self.U32 is not None:
+            _lib.call("ftl_factor_shadow", self.U[j].data_ptr(), self.dims[j] * self.R, self.U32[j].data_ptr(),
+                      self._stream(stream))
 
     def set_factor(self, j: int, U, stream=None) -> None:
         """Replace factor j (same shape) and rebuild its tree."""

@@ -137,8 +137,8 @@ def estimate_bytes(req) -> int:
         N, J = len(dims), int(req.J)
         prec = _lib.PREC[req.precision]
         total = 0
-        for I in dims:
-            total += I * R * 8 + _lib.tree_bytes(I, min(R, I), R, prec)
+        for I in dims:   # FP64 factor (+ FP32 copy in FP32 mode) and tree
+            total += I * R * (8 if prec == 0 else 12) + _lib.tree_bytes(I, min(R, I), R, prec)
         e, m, l, p = _lib.plan_sizes(N, R, prec)
         return total + e + m + l + p + N * J * 8 + J * R * 8 + J * 8 + (1 << 20)
     if isinstance(req, ALSRequest):

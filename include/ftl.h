@@ -123,7 +123,15 @@ typedef struct ftl_krp_plan {
     double *M;                           /* device workspace, (2N+3) x R x R FP64 */
     double *lambda;                      /* device workspace, (N+1) x R FP64 */
     float *pinv32;                       /* device workspace, P FP32 (FP32 weights) */
+    const float *U32[FTL_MAX_MODES];     /* optional, FP32 plans: FP32 copies of U (ftl_factor_shadow);
+                                            leaf scans then read these rows; NULL: they read U */
 } ftl_krp_plan;
+
+/* FP32 copy of a factor, out[i] = (float)U[i] for i < count.  FP32 draws whose
+ * plans carry these copies read the leaf blocks at half the bytes; results
+ * are unchanged (the leaf scan rounds the FP64 rows to FP32 anyway).  No
+ * counterpart in the reference (its sampler is FP64 only). */
+int ftl_factor_shadow(const double *U, int64_t count, float *out, void *stream);
 
 /* Sizes in bytes of the plan's workspaces. */
 int ftl_krp_plan_sizes(int N, int R, int prec, size_t *eig_bytes, size_t *M_bytes,

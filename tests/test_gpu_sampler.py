@@ -299,3 +299,44 @@ def test_pinv_square_with_nan_input_completes(ftl):
                   torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         torch.testing.assert_close(out, torch.eye(R, dtype=torch.float64, device="cuda") / 4.0)
+
+
+@pytest.mark.parametrize("R,j", [(32, 4), (64, 1), (128, 0), (25, 2)])
+def test_fp32_factor_shadows_give_identical_draws(ftl, R, j):
+    """FP32 draws whose leaf scans read the FP32 factor copies equal those
+    reading the FP64 rows, bit for bit (the scan rounds the rows to FP32
+    either way), alone and in a packed launch."""
+    rng = np.random.default_rng(50 + R)
+    dims = [3000, 2217, 4100]
+    U = [rng.normal(size=(n, R)) for n in dims]
+    U[1][rng.choice(dims[1], 40, replace=False)] *= 50.0
+    J = 6000
+    a = ftl.Sampler(U, J, R, "efficient", precision="fp32", seed=11)
+    b = ftl.Sampler(U, J, R, "efficient", precision="fp32", seed=11, factor_shadows=False)
+    assert a.U32 is not None and b.U32 is None
+    for _ in range(2):
+        sa, ha, wa = (t.clone() for t in a.draw(j))
+        sb, hb, wb = (t.clone() for t in b.draw(j))
+        assert torch.equal(sa, sb) and torch.equal(ha, hb) and torch.equal(wa, wb)
+    # packed: shadowed plans together, then a mix (falls back to FP64 rows)
+    from fast_tensor_leverage_gb300 import _lib
+    import ctypes
+    st = torch.cuda.current_stream().cuda_stream
+    for plans_of in ((a, a), (a, b)):
+        for s in plans_of:
+            _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), j, st)
+        # zeros: the excluded mode's row is left as it is, like the sampler's own buffer
+        outs = [(torch.zeros_like(s.samples_dev), torch.empty_like(s.h_dev), torch.empty_like(s.weights_dev))
+                for s in plans_of]
+        b.samples_dev.zero_()
+        n = len(plans_of)
+        _lib.call("ftl_krp_sample_packed", (ctypes.POINTER(_lib.KRPPlan) * n)(*[ctypes.pointer(s._plan) for s in plans_of]),
+                  n, (ctypes.c_uint32 * n)(*[j] * n), (ctypes.c_void_p * n)(*[o[0].data_ptr() for o in outs]),
+                  (ctypes.c_void_p * n)(*[o[1].data_ptr() for o in outs]),
+                  (ctypes.c_void_p * n)(*[o[2].data_ptr() for o in outs]), None,
+                  (ctypes.c_uint64 * n)(*[11] * n), (ctypes.c_uint64 * n)(*[0] * n), st)
+        _lib.call("ftl_krp_compute_m", ctypes.byref(b._plan), j, st)
+        _lib.call("ftl_krp_sample", ctypes.byref(b._plan), j, b.samples_dev.data_ptr(), b.h_dev.data_ptr(),
+                  b.weights_dev.data_ptr(), None, 11, 0, st)
+        for o in outs:
+            assert torch.equal(o[0], b.samples_dev) and torch.equal(o[1], b.h_dev) and torch.equal(o[2], b.weights_dev)
