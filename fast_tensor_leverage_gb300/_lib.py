@@ -70,6 +70,7 @@ _SZP = ctypes.POINTER(ctypes.c_size_t)
 SIGNATURES = {
     "ftl_last_error": ([], ctypes.c_char_p),
     "ftl_abi_version": ([], _INT),
+    "ftl_sparse_rrf": ([_P, _P, _P, _I64, _INT, _U64, ctypes.c_uint32, _P, _I64, _P], _INT),
     "ftl_factor_shadow": ([_P, _I64, _P, _P], _INT),
     "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),
     "ftl_tree_bytes": ([_I64, _I64, _INT, _INT, _SZP], _INT),

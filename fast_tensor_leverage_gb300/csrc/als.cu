@@ -404,6 +404,92 @@ __global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint
     }
 }
 
+// ---------------------------------------------------- range finder (rrf)
+
+// Standard normals of one fiber, two columns per Philox4x32-10 block:
+// block p of fiber key f in mode j = Philox(counter (f lo, f hi, p, j), key
+// seed); u1 = ((x0 >> 8) + 1) 2^-24 in (0, 1], u2 = (x1 >> 8) 2^-24 in [0, 1)
+// (exact in FP32), r = sqrt(-2 ln u1), columns 2p and 2p+1 = r cos(2 pi u2),
+// r sin(2 pi u2) (Box-Muller, FP32).
+__device__ __forceinline__ void fiber_normals(uint64_t seed, uint32_t mode, uint64_t key, uint32_t p, float &z0,
+                                              float &z1) {
+    uint32_t c[4] = {(uint32_t)key, (uint32_t)(key >> 32), p, mode};
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        philox_round(c, k);
+        k[0] += 0x9E3779B9u;
+        k[1] += 0xBB67AE85u;
+    }
+    const float u1 = (float)((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
+    const float u2 = (float)(c[1] >> 8) * (1.0f / 16777216.0f);
+    const float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    z0 = r * cs;
+    z1 = r * sn;
+}
+
+// out[idx_j(z), :] += val(z) * g(fiber(z)) over the nonzeros sorted by their
+// mode-j index (SortIdxLookup::execute_rrf, sort_lookup.hpp:262-353: one
+// Gaussian R-vector per fiber).  Chunks of MTT_CHUNK nonzeros per warp, lane
+// l owns column pairs l, l + 32, ...; per-row accumulation, one atomic add
+// per column when the row changes.
+constexpr int RRF_CHUNK = 512;
+
+__global__ void rrf_rows_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
+                                const double *__restrict__ rvals, int64_t nnz, int R, uint64_t seed, uint32_t mode,
+                                double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    constexpr int PPL = (FTL_MAX_RANK / 2 + 31) / 32;  // column pairs per lane
+    const int npairs = (R + 1) / 2;
+    const int64_t nchunks = (nnz + RRF_CHUNK - 1) / RRF_CHUNK;
+    for (int64_t ch = gw; ch < nchunks; ch += nw) {
+        const int64_t z0 = ch * RRF_CHUNK, z1 = min(nnz, z0 + RRF_CHUNK);
+        double acc[2 * PPL];
+#pragma unroll
+        for (int c = 0; c < 2 * PPL; ++c) acc[c] = 0.0;
+        int32_t cur = -1;
+        for (int64_t z = z0; z < z1; ++z) {
+            const int32_t row = rrows[z];
+            const uint64_t key = rkeys[z];
+            const double v = rvals[z];
+            if (row != cur) {
+                if (cur >= 0) {
+#pragma unroll
+                    for (int q = 0; q < PPL; ++q) {
+                        const int pp = lane + 32 * q;
+                        if (2 * pp < R) atomicAdd(out + (int64_t)cur * R + 2 * pp, acc[2 * q]);
+                        if (2 * pp + 1 < R) atomicAdd(out + (int64_t)cur * R + 2 * pp + 1, acc[2 * q + 1]);
+                        acc[2 * q] = acc[2 * q + 1] = 0.0;
+                    }
+                }
+                cur = row;
+            }
+#pragma unroll
+            for (int q = 0; q < PPL; ++q) {
+                const int pp = lane + 32 * q;
+                if (pp < npairs) {
+                    float g0, g1;
+                    fiber_normals(seed, mode, key, (uint32_t)pp, g0, g1);
+                    acc[2 * q] = fma(v, (double)g0, acc[2 * q]);
+                    acc[2 * q + 1] = fma(v, (double)g1, acc[2 * q + 1]);
+                }
+            }
+        }
+        if (cur >= 0) {
+#pragma unroll
+            for (int q = 0; q < PPL; ++q) {
+                const int pp = lane + 32 * q;
+                if (2 * pp < R) atomicAdd(out + (int64_t)cur * R + 2 * pp, acc[2 * q]);
+                if (2 * pp + 1 < R) atomicAdd(out + (int64_t)cur * R + 2 * pp + 1, acc[2 * q + 1]);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------ solve / renorm
 
 // U = B pinv (pinv R x R symmetric) row by row; an all-zero row of B (a row
@@ -821,4 +907,19 @@ extern "C" int ftl_sparse_exact_mttkrp(const uint32_t *idx, const double *vals, 
     if (nnz == 0) return FTL_OK;
     exact_mttkrp_kernel<<<num_sms() * 16, 256, 0, st>>>(idx, vals, nnz, N, j, fp, R, out);
     return check_launch("exact_mttkrp_kernel");
+}
+
+extern "C" int ftl_sparse_rrf(const int32_t *row_idx, const uint64_t *row_keys, const double *row_vals, int64_t nnz,
+                              int R, uint64_t seed, uint32_t mode, double *out, int64_t I_j, void *stream) {
+    FTL_CHECK_ARG(row_idx && row_keys && row_vals && out, "ftl_sparse_rrf: null pointer");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1 && nnz >= 0, "ftl_sparse_rrf: bad shape R=%d I_j=%lld",
+                  R, (long long)I_j);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t err = cudaMemsetAsync(out, 0, (size_t)I_j * R * sizeof(double), st);
+    if (err != cudaSuccess) return fail(FTL_E_CUDA, "ftl_sparse_rrf: memset: %s", cudaGetErrorString(err));
+    if (nnz == 0) return FTL_OK;
+    const int64_t nchunks = (nnz + RRF_CHUNK - 1) / RRF_CHUNK;
+    int blocks = (int)std::min<int64_t>((nchunks * 32 + 255) / 256, (int64_t)num_sms() * 32);
+    rrf_rows_kernel<<<std::max(blocks, 1), 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, R, seed, mode, out);
+    return check_launch("rrf_rows_kernel");
 }

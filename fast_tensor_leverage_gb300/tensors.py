@@ -279,6 +279,26 @@ class SparseTensor:
                   terms[1:2].data_ptr(), st)
         return terms
 
+    def execute_rrf(self, lr: "LowRankTensor", seed: int | None = None) -> None:
+        """Randomized range-finder initialisation of `lr` (SparseTensor::
+        execute_rrf, sparse_tensor.hpp:84-92): for every mode j, U_j = X_(j)
+        Omega_j with one N(0,1) R-vector per fiber of mode j, then
+        lr.renormalize_columns(-1).  The vectors come from a counter-based
+        generator keyed by `seed` (random when None, as in the reference)."""
+        import secrets
+        if lr.N != self.N or lr.device != self.device:
+            raise ValueError("tensor and decomposition disagree on modes or device")
+        for k in range(self.N):
+            if self.dims[k] > lr.dims[k]:
+                raise ValueError(f"mode {k}: tensor index range {self.dims[k]} exceeds factor rows {lr.dims[k]}")
+        seed = secrets.randbits(63) if seed is None else int(seed)
+        st = D.stream_ptr(self.device)
+        for j in range(self.N):
+            rrows, rkeys, rvals = self.rows[j]
+            _lib.call("ftl_sparse_rrf", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), self.nnz, lr.R,
+                      seed, j, lr.U_dev[j].data_ptr(), lr.dims[j], st)
+        lr.renormalize_columns(-1)
+
     def execute_downsampled_mttkrp_py(self, samples, lhs, j: int, result) -> None:
         """result (I_j x R) = sum over the rows i of samples (J x N uint64) of
         the fiber of samples[i] (modes != j) times lhs[i]

@@ -272,6 +272,18 @@ int ftl_sparse_exact_mttkrp(const uint32_t *idx_dev, const double *vals_dev, int
                             int j, const double *const *U_dev, int R, double *out_dev,
                             int64_t I_j, void *stream);
 
+/* Randomized range finder of mode j (SortIdxLookup::execute_rrf,
+ * cpp_ext/sort_lookup.hpp:262-353): out (I_j x R, zeroed first) = X_(j) Omega,
+ * Omega holding one N(0,1) R-vector per fiber (modes != j).  Inputs are the
+ * nonzeros sorted by their mode-j index (row index, fiber key, value, as for
+ * ftl_sparse_mttkrp_rows).  The reference draws from unseeded per-thread
+ * generators; here fiber f's vector is Philox4x32-10 (counter (f lo, f hi,
+ * column pair p, mode), key seed) through Box-Muller in FP32: u1 = ((x0 >> 8)
+ * + 1) 2^-24, u2 = (x1 >> 8) 2^-24, columns 2p, 2p+1 = sqrt(-2 ln u1)
+ * (cos, sin)(2 pi u2).  Reproducible and independent of the launch shape. */
+int ftl_sparse_rrf(const int32_t *row_idx, const uint64_t *row_keys, const double *row_vals, int64_t nnz,
+                   int R, uint64_t seed, uint32_t mode, double *out, int64_t I_j, void *stream);
+
 /* out_mat (R x R) = (sigma_a sigma_b^T) o prod_{k != exclude} G_k over N full
  * R x R FP64 Grams (host array of device pointers; exclude = -1 for none; a
  * NULL sigma means all ones); out_sum = sum of its entries.  Either output

@@ -352,3 +352,39 @@ class OracleALS:
         for k in range(self.N):
             G = G * (self.U[k].T @ self.U[k])
         return float(np.sum(self.vals ** 2 - 2 * self.vals * m) + G.sum())
+
+
+def fiber_normals(seed: int, mode: int, key: int, R: int) -> np.ndarray:
+    """The R standard normals of one fiber in the GPU range finder
+    (ftl_sparse_rrf): Philox4x32-10 block p = (counter (key lo, key hi, p,
+    mode), key seed), u1 = ((x0 >> 8) + 1) 2^-24, u2 = (x1 >> 8) 2^-24,
+    columns 2p, 2p+1 = sqrt(-2 ln u1) (cos, sin)(2 pi u2), here in FP64."""
+    out = np.empty(2 * ((R + 1) // 2))
+    kk = [seed & 0xFFFFFFFF, seed >> 32]
+    for p in range((R + 1) // 2):
+        x = philox4x32_10([key & 0xFFFFFFFF, key >> 32, p, mode], kk)
+        u1 = ((x[0] >> 8) + 1) / 16777216.0
+        u2 = (x[1] >> 8) / 16777216.0
+        r = np.sqrt(-2.0 * np.log(u1))
+        out[2 * p], out[2 * p + 1] = r * np.cos(2 * np.pi * u2), r * np.sin(2 * np.pi * u2)
+    return out[:R]
+
+
+def rrf(idx: np.ndarray, vals: np.ndarray, dims, rows, R: int, seed: int) -> list:
+    """Restatement of SparseTensor::execute_rrf (sparse_tensor.hpp:84-92,
+    sort_lookup.hpp:262-353) before the final renormalisation: for every mode
+    j, U_j[idx_j] += v * g(fiber), one Gaussian vector per fiber (the modes
+    != j), with the GPU's counter-based vectors; `rows` = factor row counts."""
+    idx = np.asarray(idx, dtype=np.int64)
+    out = []
+    for j in range(len(dims)):
+        keys = fiber_keys(idx, dims, j)
+        U = np.zeros((rows[j], R))
+        cache = {}
+        for z in range(idx.shape[0]):
+            k = int(keys[z])
+            if k not in cache:
+                cache[k] = fiber_normals(seed, j, k, R)
+            U[idx[z, j]] += vals[z] * cache[k]
+        out.append(U)
+    return out

@@ -193,3 +193,42 @@ def test_gpu_exact_als_update_rank128_matches_numpy(ftl):
     norms[norms <= 1e-7] = 1.0
     np.testing.assert_allclose(U[j], Uj / norms, rtol=0, atol=1e-8 * np.abs(Uj / norms).max())
     np.testing.assert_allclose(lr.sigma, norms, rtol=1e-8)
+
+
+def test_gpu_rrf_matches_oracle_and_is_gaussian(ftl):
+    """SparseTensor.execute_rrf: the range finder of every mode against the
+    oracle restatement with the same counter-based Gaussian vectors (FP32
+    Box-Muller on the GPU vs FP64 in the oracle: 1e-5 of the largest entry),
+    then unit columns and sigma = product of the column norms."""
+    c = load_als(als_cases()[1])
+    R, seed = 9, 77
+    rows = [d + 3 for d in c["dims"]]          # factors may have more rows than the tensor
+    U = [np.zeros((r, R)) for r in rows]
+    lr = ftl.LowRankTensor(R, U)
+    sp = ftl.SparseTensor(c["idx"], c["vals"], "sort", dims=c["dims"])
+    sp.execute_rrf(lr, seed=seed)
+    Uo = O.rrf(c["idx"], c["vals"], c["dims"], rows, R, seed)
+    sig = np.ones(R)
+    for k in range(c["N"]):
+        n = np.linalg.norm(Uo[k], axis=0)
+        n[n <= 1e-7] = 1.0
+        sig *= n
+        np.testing.assert_allclose(U[k], Uo[k] / n, rtol=0, atol=1e-5)
+        assert np.all(U[k][c["dims"][k]:] == 0.0)
+    np.testing.assert_allclose(lr.sigma, sig, rtol=1e-5)
+    # one nonzero of value 1 per row, all in distinct fibers: rows = the vectors
+    n_rows, R2 = 20000, 64
+    idx = np.stack([np.arange(n_rows), np.arange(n_rows) % 97, np.arange(n_rows) // 97], axis=1).astype(np.uint32)
+    sp2 = ftl.SparseTensor(idx, np.ones(n_rows), "sort", dims=[n_rows, 97, n_rows // 97 + 1])
+    out = torch.empty((n_rows, R2), dtype=torch.float64, device="cuda")
+    from fast_tensor_leverage_gb300 import _lib
+    rrows, rkeys, rvals = sp2.rows[0]
+    _lib.call("ftl_sparse_rrf", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), sp2.nnz, R2, 5, 0,
+              out.data_ptr(), n_rows, torch.cuda.current_stream().cuda_stream)
+    g = out.cpu().numpy()
+    assert abs(g.mean()) < 0.005 and abs(g.var() - 1.0) < 0.01
+    assert abs(((g - g.mean()) ** 4).mean() / g.var() ** 2 - 3.0) < 0.05
+    corr = np.corrcoef(g[:, :8].T)
+    assert np.abs(corr - np.eye(8)).max() < 0.05
+    ref = np.stack([O.fiber_normals(5, 0, int(k), R2) for k in rkeys[:50].cpu().numpy()])
+    np.testing.assert_allclose(g[rrows[:50].cpu().numpy()], ref, rtol=0, atol=1e-5)

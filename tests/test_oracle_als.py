@@ -55,3 +55,66 @@ def test_oracle_als_matches_live_reference():
     s2 = np.zeros(R)
     lr.get_sigma(s2, -1)
     np.testing.assert_allclose(o.residual_normsq(), sp.compute_residual_normsq(s2, U), rtol=1e-11)
+
+
+def _rrf_tensor(rng):
+    """3-mode tensor whose mode-0 unfolding has few fibers: 6 (i1, i2)
+    fibers, each holding several mode-0 rows; rows 0..3 of mode 0 are
+    empty; rows 4..9 have exactly one nonzero, pairs (4,5), (6,7) share a
+    fiber."""
+    dims = [30, 12, 9]
+    fibers = [(1, 2), (3, 4), (5, 0), (7, 8), (11, 1), (0, 6)]
+    entries = {}
+    for r, f in [(4, 0), (5, 0), (6, 1), (7, 1), (8, 2), (9, 3)]:
+        entries[(r,) + fibers[f]] = rng.random() + 0.5
+    for r in range(10, 30):
+        for f in rng.choice(6, size=2, replace=False):
+            entries[(r,) + fibers[f]] = rng.random() + 0.5
+    idx = np.array(list(entries.keys()), dtype=np.uint32)
+    vals = np.array(list(entries.values()))
+    return dims, idx, vals, fibers
+
+
+def check_rrf_structure(U0, dims, idx, vals, fibers):
+    v = {tuple(int(a) for a in t): x for t, x in zip(idx, vals)}
+    assert np.all(U0[:4] == 0.0)
+    for (a, b, f) in [(4, 5, 0), (6, 7, 1)]:
+        va, vb = v[(a,) + fibers[f]], v[(b,) + fibers[f]]
+        np.testing.assert_allclose(U0[a] / va, U0[b] / vb, rtol=1e-12, atol=1e-15)
+    # columns of U_0 lie in the 6-dimensional range of X_(0)
+    X = np.zeros((dims[0], len(fibers)))
+    for t, x in v.items():
+        X[t[0], fibers.index(t[1:])] = x
+    Q, _ = np.linalg.qr(X)
+    resid = U0 - Q @ (Q.T @ U0)
+    assert np.abs(resid).max() < 1e-12 * max(1.0, np.abs(U0).max())
+    np.testing.assert_allclose(np.linalg.norm(U0, axis=0), 1.0, rtol=1e-12)
+
+
+def test_rrf_structure_of_reference_and_oracle():
+    """execute_rrf (sort_lookup.hpp:262-353): one Gaussian vector per fiber,
+    summed over each row's nonzeros, then unit columns.  The reference draws
+    from unseeded generators, so it is pinned by properties that hold for
+    every draw; the oracle restatement (with the GPU's counter-based
+    vectors) must show the same structure."""
+    rng = np.random.default_rng(5)
+    dims, idx, vals, fibers = _rrf_tensor(rng)
+    R = 40
+    ref_dir = REPO / "oracle" / "_ref"
+    if list(ref_dir.glob("ftl_ref*.so")):
+        sys.path.insert(0, str(ref_dir))
+        import ftl_ref
+        U = [np.zeros((d, R)) for d in dims]
+        lr = ftl_ref.LowRankTensor(R, U)
+        sp = ftl_ref.SparseTensor(idx, vals, "sort")
+        sp.execute_rrf(lr)
+        check_rrf_structure(U[0], dims, idx, vals, fibers)
+    Uo = O.rrf(idx, vals, dims, dims, R, seed=123)
+    Uo = [u / np.where(np.linalg.norm(u, axis=0) <= 1e-7, 1.0, np.linalg.norm(u, axis=0)) for u in Uo]
+    check_rrf_structure(Uo[0], dims, idx, vals, fibers)
+
+
+def test_fiber_normals_are_standard_normal():
+    g = np.concatenate([O.fiber_normals(9, 1, k * 7919 + 3, 64) for k in range(400)])
+    assert abs(g.mean()) < 0.02 and abs(g.var() - 1.0) < 0.03
+    assert abs(((g - g.mean()) ** 4).mean() / g.var() ** 2 - 3.0) < 0.15
