@@ -70,6 +70,20 @@ _SZP = ctypes.POINTER(ctypes.c_size_t)
 SIGNATURES = {
     "ftl_last_error": ([], ctypes.c_char_p),
     "ftl_abi_version": ([], _INT),
+    "ftl_lowrank_mttkrp_workspace_bytes": ([_INT, _INT, _P], _INT),
+    "ftl_lowrank_sampled_mttkrp": ([_P, _P, _INT, _INT, _INT, _P, _I64, _P, _P, _P, _I64, _P, _P, _INT, _P,
+                                    ctypes.c_size_t, _P, _I64, _I64, _P], _INT),
+    "ftl_dense_sampled_mttkrp": ([_P, _INT, _P, _INT, _INT, _P, _I64, _P, _P, _P, _I64, _P, _P, _INT, _P, _I64,
+                                  _P], _INT),
+    "ftl_dense_materialize": ([_P, _INT, _P, _INT, _INT, _P, _I64, _P, _P], _INT),
+    "ftl_dense_residual_workspace_bytes": ([_P], _INT),
+    "ftl_dense_residual_terms": ([_P, _INT, _P, _INT, _P, _P, _INT, _P, ctypes.c_size_t, _P, _P], _INT),
+    "ftl_lowrank_evaluate": ([_P, _INT, _INT, _P, _P, _INT, _I64, _P, _P], _INT),
+    "ftl_lowrank_materialize": ([_P, _INT, _INT, _P, _P, _I64, _INT, _I64, _P, _P], _INT),
+    "ftl_cross_gram_workspace_bytes": ([_INT, _INT, _P], _INT),
+    "ftl_cross_gram": ([_P, _INT, _P, _INT, _I64, _P, ctypes.c_size_t, _P, _P], _INT),
+    "ftl_chain_prod": ([_P, _INT, _INT, _INT, _INT, _P, _P, _P, _P, _P], _INT),
+    "ftl_rows_times": ([_P, _I64, _INT, _P, _INT, _P, _I64, _P], _INT),
     "ftl_sparse_rrf": ([_P, _P, _P, _I64, _INT, _U64, ctypes.c_uint32, _P, _I64, _P], _INT),
     "ftl_factor_shadow": ([_P, _I64, _P, _P], _INT),
     "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),

@@ -25,15 +25,18 @@ import torch
 from . import _device as D
 from . import _lib
 from .sampler import Sampler
-from .tensors import LowRankTensor, SparseTensor, _ptrs, _Workspace, factor_gram
+from .tensors import DenseTensor, LowRankTensor, SparseTensor, _ptrs, _Workspace, factor_gram
 
 
 class ALS:
     def __init__(self, cp_decomp: LowRankTensor, ground_truth: SparseTensor):
         if not isinstance(cp_decomp, LowRankTensor):
             raise TypeError("cp_decomp must be a fast_tensor_leverage_gb300.LowRankTensor")
-        if not isinstance(ground_truth, SparseTensor):
-            raise TypeError("ground_truth must be a fast_tensor_leverage_gb300.SparseTensor")
+        if not isinstance(ground_truth, (SparseTensor, LowRankTensor, DenseTensor)):
+            raise TypeError("ground_truth must be a SparseTensor, LowRankTensor or DenseTensor "
+                            "of fast_tensor_leverage_gb300")
+        if ground_truth is cp_decomp:
+            raise ValueError("the decomposition cannot be its own ground truth")
         if ground_truth.N != cp_decomp.N:
             raise ValueError("tensor and decomposition disagree on the number of modes")
         for k in range(cp_decomp.N):
@@ -78,6 +81,8 @@ class ALS:
         # every buffer an update uses is sized here, so updates (and captured
         # sweeps) allocate nothing
         self._ws.get("dedup", _lib.ws_bytes("dedup", J))
+        if isinstance(self.ground_truth, LowRankTensor):
+            self.ground_truth._ws.get("lowrank_mttkrp", _lib.ws_bytes("lowrank_mttkrp", self.ground_truth.R, R))
         self._ws.get("gram", _lib.ws_bytes("gram", R))
         lr._ws.get("colnorm", _lib.ws_bytes("colnorm", R))
         if getattr(lr, "_norms", None) is None:
@@ -108,7 +113,12 @@ class ALS:
                   self._pinv.data_ptr(), self._vscr.data_ptr(), st)
         I_j = lr.dims[j]
         mt = self._mttkrp[: I_j * R]
-        if I_j == gt.dims[j]:
+        if not isinstance(gt, SparseTensor):
+            # black-box right-hand side (black_box_tensor.hpp:21-67): low-rank
+            # shortcut or dense fiber gather, rows past gt.dims[j] zeroed
+            gt._sampled_mttkrp_dev(samples.data_ptr(), J, self._urep.data_ptr(), self._ucnt.data_ptr(),
+                                   self._nuniq.data_ptr(), w.data_ptr(), h.data_ptr(), R, j, mt.data_ptr(), I_j, st)
+        elif I_j == gt.dims[j]:
             # one balanced pass over the nonzeros sorted by output row
             rrows, rkeys, rvals = gt.rows[j]
             _lib.call("ftl_sparse_mttkrp_rows", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), gt.nnz,
@@ -144,8 +154,10 @@ class ALS:
         _lib.call("ftl_pinv_square", gram.data_ptr(), R, R, None, 1e-11, pinv.data_ptr(), vscr.data_ptr(), st)
         I_j = lr.dims[j]
         mt = torch.empty((I_j, R), dtype=torch.float64, device=self.device)
-        _lib.call("ftl_sparse_exact_mttkrp", gt.idx_dev.data_ptr(), gt.vals_dev.data_ptr(), gt.nnz, N, j,
-                  _ptrs(lr.U_dev), R, mt.data_ptr(), I_j, st)
+        if isinstance(gt, DenseTensor):
+            # the reference's DenseTensor has no exact MTTKRP (tensor.hpp:21-23 leaves it empty)
+            raise NotImplementedError("exact ALS updates against a DenseTensor are not supported")
+        gt._exact_mttkrp_dev(lr.U_dev, j, mt.data_ptr(), I_j, st)
         _lib.call("ftl_solve_rows", mt.data_ptr(), pinv.data_ptr(), I_j, R, lr.U_dev[j].data_ptr(), st)
         if renormalize:
             lr.renormalize_columns(j)
@@ -209,6 +221,16 @@ class ALS:
 
 
 # ------------------------------------------------------------ Python driver
+
+class PyDenseTensor:
+    """The reference's PyDenseTensor (tensors.py:122-130): a dense array as
+    an ALS right-hand side (FP32 or FP64, kept in its precision)."""
+
+    def __init__(self, data):
+        self.ten = DenseTensor(data, 10000)
+        self.N = self.ten.N
+        self.dims = list(self.ten.dims)
+
 
 class PyLowRank:
     """The reference's PyLowRank (tensors.py:16-53): Gaussian factors from

@@ -170,6 +170,225 @@ class LowRankTensor:
         return self._normsq
 
 
+# --------------------------------------------------- low-rank as a tensor
+# (LowRankTensor as the right-hand side of ALS or a fit; the reference's
+# BlackBoxTensor / Tensor interface, cpp_ext/low_rank_tensor.hpp:70-280)
+
+def _lr_other(lr, sigma, U_list, R):
+    st = D.stream_ptr(lr.device)
+    if isinstance(sigma, torch.Tensor):
+        sig = sigma.to(lr.device, torch.float64).contiguous()
+    else:
+        sig = torch.from_numpy(np.ascontiguousarray(np.asarray(sigma, dtype=np.float64).reshape(-1)[:R])).to(lr.device)
+    Ud = []
+    for k, u in enumerate(U_list):
+        if isinstance(u, torch.Tensor) and u.is_cuda:
+            Ud.append(u.to(lr.device, torch.float64).contiguous())
+        else:
+            Ud.append(torch.from_numpy(D.as_factor(u, R, f"U[{k}]")).to(lr.device))
+    return st, sig, Ud
+
+
+def _chain_sum(ws, st, A, Ra, sa, B, Rb, sb) -> torch.Tensor:
+    """sum_rs sa_r sb_s prod_k (A_k^T B_k)_rs on the device (ATB_chain_prod_sum)."""
+    dev = A[0].device
+    nb = _lib.ws_bytes("cross_gram", Ra, Rb)
+    w = ws.get("cross", nb)
+    G = []
+    for a, b in zip(A, B):
+        g = torch.empty((Ra, Rb), dtype=torch.float64, device=dev)
+        _lib.call("ftl_cross_gram", a.data_ptr(), Ra, b.data_ptr(), Rb, a.shape[0], w.data_ptr(), nb, g.data_ptr(), st)
+        G.append(g)
+    out = torch.empty(1, dtype=torch.float64, device=dev)
+    _lib.call("ftl_chain_prod", _ptrs(G), len(G), Ra, Rb, -1, sa.data_ptr(), sb.data_ptr(), None, out.data_ptr(), st)
+    return out
+
+
+def _lr_compute_residual_normsq(self, sigma, U_list) -> float:
+    """||self - [[sigma; U]]||^2 = ||self||^2 + ||other||^2 - 2 <other, self>
+    by Gram chains (LowRankTensor::compute_residual_normsq,
+    low_rank_tensor.hpp:78-89), clamped at 0 like the reference."""
+    Ro = len(np.asarray(sigma).reshape(-1)) if not isinstance(sigma, torch.Tensor) else int(sigma.numel())
+    st, sig, Ud = _lr_other(self, sigma, U_list, Ro)
+    t_self = _chain_sum(self._ws, st, self.U_dev, self.R, self.sigma_dev, self.U_dev, self.R, self.sigma_dev)
+    t_other = _chain_sum(self._ws, st, Ud, Ro, sig, Ud, Ro, sig)
+    t_cross = _chain_sum(self._ws, st, Ud, Ro, sig, self.U_dev, self.R, self.sigma_dev)
+    v = torch.cat([t_self, t_other, t_cross]).cpu().numpy()
+    return max(float(v[0] + v[1] - 2.0 * v[2]), 0.0)
+
+
+def _lr_evaluate_indices(self, indices, result) -> None:
+    """result[z] = sum_r sigma_r prod_k U_k[indices[z, k], r]
+    (LowRankTensor::evaluate_indices, low_rank_tensor.hpp:262-280)."""
+    idx = np.ascontiguousarray(np.asarray(indices, dtype=np.uint32))
+    n = idx.shape[0]
+    out = D.require_numpy_out(result, np.float64, "result", min_size=n)
+    if idx.ndim != 2 or idx.shape[1] != self.N:
+        raise ValueError(f"indices must be (n, {self.N})")
+    idx_d = torch.from_numpy(idx.view(np.int32)).to(self.device)
+    o = torch.empty(n, dtype=torch.float64, device=self.device)
+    _lib.call("ftl_lowrank_evaluate", _ptrs(self.U_dev), self.N, self.R, self.sigma_dev.data_ptr(), idx_d.data_ptr(),
+              0, n, o.data_ptr(), D.stream_ptr(self.device))
+    out.reshape(-1)[:n] = o.cpu().numpy()
+
+
+def _lr_materialize_rhs(self, samples, j: int, rhs_buf) -> None:
+    """Fibers at the samples (n x N uint64): j >= N: rhs_buf (n x R) = sigma o
+    prod_k U_k[s_k]; else rhs_buf (n x I_j) = that row times U_j^T
+    (LowRankTensor::materialize_rhs, low_rank_tensor.hpp:91-135)."""
+    S = np.ascontiguousarray(np.asarray(samples, dtype=np.uint64))
+    n, j = S.shape[0], int(j)
+    cols = self.R if j >= self.N else self.dims[j]
+    out = D.require_numpy_out(rhs_buf, np.float64, "rhs_buf", min_size=n * cols)
+    S_d = torch.from_numpy(S.view(np.int64)).to(self.device)
+    o = torch.empty((n, cols), dtype=torch.float64, device=self.device)
+    _lib.call("ftl_lowrank_materialize", _ptrs(self.U_dev), self.N, self.R, self.sigma_dev.data_ptr(), S_d.data_ptr(),
+              n, j, self.dims[j] if j < self.N else 0, o.data_ptr(), D.stream_ptr(self.device))
+    out.reshape(-1)[: n * cols] = o.cpu().numpy().reshape(-1)
+
+
+def _lr_sampled_mttkrp_dev(self, samples, J, urep, ucnt, nuniq, w, h, R, j, out, out_rows, stream) -> None:
+    nb = _lib.ws_bytes("lowrank_mttkrp", self.R, R)
+    ws = self._ws.get("lowrank_mttkrp", nb)
+    _lib.call("ftl_lowrank_sampled_mttkrp", _ptrs(self.U_dev), self.sigma_dev.data_ptr(), self.N, self.R, j,
+              samples, J, urep, ucnt, nuniq, J, w, h, R, ws.data_ptr(), nb, out, self.dims[j], out_rows, stream)
+
+
+def _lr_execute_downsampled_mttkrp_py(self, samples, lhs, j: int, result) -> None:
+    """result (I_j x R) = sum over the rows s of samples (J x N uint64) of
+    fiber_s (x) lhs[s] (BlackBoxTensor::execute_downsampled_mttkrp,
+    black_box_tensor.hpp:21-67), through the low-rank shortcut."""
+    S = np.ascontiguousarray(np.asarray(samples, dtype=np.uint64))
+    L = np.ascontiguousarray(np.asarray(lhs, dtype=np.float64))
+    J, R = L.shape
+    out = D.require_numpy_out(result, np.float64, "result", min_size=self.dims[j] * R)
+    S_d = torch.from_numpy(np.ascontiguousarray(S.T).view(np.int64)).to(self.device)   # N x J
+    L_d = torch.from_numpy(L).to(self.device)
+    o = torch.empty((self.dims[j], R), dtype=torch.float64, device=self.device)
+    _lr_sampled_mttkrp_dev(self, S_d.data_ptr(), J, None, None, None, None, L_d.data_ptr(), R, int(j), o.data_ptr(),
+                           self.dims[j], D.stream_ptr(self.device))
+    out.reshape(-1)[: self.dims[j] * R] = o.cpu().numpy().reshape(-1)
+
+
+def _lr_exact_mttkrp_dev(self, U_L, j: int, out, out_rows, stream) -> None:
+    """out = U_j (sigma 1^T o prod_{k != j} U_k^T U_L,k)
+    (LowRankTensor::execute_exact_mttkrp, low_rank_tensor.hpp:147-180)."""
+    R_L = int(U_L[0].shape[1])
+    nb = _lib.ws_bytes("cross_gram", self.R, R_L)
+    w = self._ws.get("cross", nb)
+    G = []
+    for k in range(self.N):
+        g = torch.empty((self.R, R_L), dtype=torch.float64, device=self.device)
+        if k != j:
+            _lib.call("ftl_cross_gram", self.U_dev[k].data_ptr(), self.R, U_L[k].data_ptr(), R_L, self.dims[k],
+                      w.data_ptr(), nb, g.data_ptr(), stream)
+        G.append(g)
+    M = torch.empty((self.R, R_L), dtype=torch.float64, device=self.device)
+    _lib.call("ftl_chain_prod", _ptrs(G), self.N, self.R, R_L, j, self.sigma_dev.data_ptr(), None, M.data_ptr(),
+              None, stream)
+    _lib.call("ftl_rows_times", self.U_dev[j].data_ptr(), self.dims[j], self.R, M.data_ptr(), R_L, out, out_rows,
+              stream)
+
+
+LowRankTensor.compute_residual_normsq = _lr_compute_residual_normsq
+LowRankTensor.evaluate_indices = _lr_evaluate_indices
+LowRankTensor.materialize_rhs = _lr_materialize_rhs
+LowRankTensor.execute_downsampled_mttkrp_py = _lr_execute_downsampled_mttkrp_py
+LowRankTensor._sampled_mttkrp_dev = _lr_sampled_mttkrp_dev
+LowRankTensor._exact_mttkrp_dev = _lr_exact_mttkrp_dev
+
+
+class DenseTensor:
+    """Dense row-major tensor (FP64 or FP32) resident on the device, usable
+    as the right-hand side of ALS (DenseTensor<VAL_T>,
+    cpp_ext/dense_tensor.hpp:13-59).  `data`: numpy array or CUDA tensor.
+    Unlike the reference (whose DenseTensor has no residual), get_normsq and
+    compute_residual_normsq are implemented."""
+
+    def __init__(self, data, max_rhs_rows: int = 10000, *, device=None):
+        self.device = D.cuda_device(device)
+        if isinstance(data, torch.Tensor):
+            t = data.to(self.device).contiguous()
+        else:
+            a = np.asarray(data)
+            if a.dtype not in (np.float32, np.float64):
+                a = a.astype(np.float64)
+            t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+        if t.dtype not in (torch.float32, torch.float64):
+            t = t.to(torch.float64)
+        self.T_dev = t
+        self.is_f32 = t.dtype == torch.float32
+        self.dims = [int(d) for d in t.shape]
+        self.N = len(self.dims)
+        self.max_rhs_rows = int(max_rhs_rows)
+        self._dims_c = (ctypes.c_int64 * self.N)(*self.dims)
+        self._ws = _Workspace(self.device)
+        self._normsq = None
+
+    def _terms(self, sigma, U_list, R):
+        st = D.stream_ptr(self.device)
+        nb = _lib.ws_bytes("dense_residual")
+        out = torch.empty(2, dtype=torch.float64, device=self.device)
+        if U_list is None:
+            _lib.call("ftl_dense_residual_terms", self.T_dev.data_ptr(), int(self.is_f32), self._dims_c, self.N, None,
+                      None, 1, self._ws.get("dense", nb).data_ptr(), nb, out.data_ptr(), st)
+        else:
+            _, sig, Ud = _lr_other(self, sigma, U_list, R)
+            _lib.call("ftl_dense_residual_terms", self.T_dev.data_ptr(), int(self.is_f32), self._dims_c, self.N,
+                      _ptrs(Ud), sig.data_ptr(), R, self._ws.get("dense", nb).data_ptr(), nb, out.data_ptr(), st)
+        return out.cpu().numpy()
+
+    def get_normsq(self) -> float:
+        if self._normsq is None:
+            self._normsq = float(self._terms(None, None, 1)[1])
+        return self._normsq
+
+    def compute_residual_normsq(self, sigma, U_list) -> float:
+        R = int(sigma.numel()) if isinstance(sigma, torch.Tensor) else len(np.asarray(sigma).reshape(-1))
+        return float(self._terms(sigma, U_list, R)[0])
+
+    def materialize_rhs(self, samples, j: int, rhs_buf) -> None:
+        """rhs_buf (n x I_j) = the fibers at the samples (n x N uint64)
+        (DenseTensor::materialize_rhs, dense_tensor.hpp:38-59)."""
+        S = np.ascontiguousarray(np.asarray(samples, dtype=np.uint64))
+        n, j = S.shape[0], int(j)
+        out = D.require_numpy_out(rhs_buf, np.float64, "rhs_buf", min_size=n * self.dims[j])
+        S_d = torch.from_numpy(S.view(np.int64)).to(self.device)
+        o = torch.empty((n, self.dims[j]), dtype=torch.float64, device=self.device)
+        _lib.call("ftl_dense_materialize", self.T_dev.data_ptr(), int(self.is_f32), self._dims_c, self.N, j,
+                  S_d.data_ptr(), n, o.data_ptr(), D.stream_ptr(self.device))
+        out.reshape(-1)[: n * self.dims[j]] = o.cpu().numpy().reshape(-1)
+
+    def _sampled_mttkrp_dev(self, samples, J, urep, ucnt, nuniq, w, h, R, j, out, out_rows, stream) -> None:
+        _lib.call("ftl_dense_sampled_mttkrp", self.T_dev.data_ptr(), int(self.is_f32), self._dims_c, self.N, j,
+                  samples, J, urep, ucnt, nuniq, J, w, h, R, out, out_rows, stream)
+
+    def execute_downsampled_mttkrp_py(self, samples, lhs, j: int, result) -> None:
+        """result (I_j x R) = sum over the rows s of samples (J x N uint64) of
+        fiber_s (x) lhs[s] (BlackBoxTensor::execute_downsampled_mttkrp)."""
+        S = np.ascontiguousarray(np.asarray(samples, dtype=np.uint64))
+        L = np.ascontiguousarray(np.asarray(lhs, dtype=np.float64))
+        J, R = L.shape
+        out = D.require_numpy_out(result, np.float64, "result", min_size=self.dims[j] * R)
+        S_d = torch.from_numpy(np.ascontiguousarray(S.T).view(np.int64)).to(self.device)
+        L_d = torch.from_numpy(L).to(self.device)
+        o = torch.empty((self.dims[j], R), dtype=torch.float64, device=self.device)
+        self._sampled_mttkrp_dev(S_d.data_ptr(), J, None, None, None, None, L_d.data_ptr(), R, int(j), o.data_ptr(),
+                                 self.dims[j], D.stream_ptr(self.device))
+        out.reshape(-1)[: self.dims[j] * R] = o.cpu().numpy().reshape(-1)
+
+
+def DenseTensor_double(data, max_rhs_rows: int = 10000):
+    """The reference's DenseTensor_double binding (als_module.cpp:99-100)."""
+    return DenseTensor(np.asarray(data, dtype=np.float64), max_rhs_rows)
+
+
+def DenseTensor_float(data, max_rhs_rows: int = 10000):
+    """The reference's DenseTensor_float binding (als_module.cpp:101-102)."""
+    return DenseTensor(np.asarray(data, dtype=np.float32), max_rhs_rows)
+
+
+
 class SparseTensor:
     """COO tensor with one sorted fiber lookup per mode
     (SparseTensor, sparse_tensor.hpp:46-77; SortIdxLookup ctor,
@@ -278,6 +497,11 @@ class SparseTensor:
         _lib.call("ftl_gram_hadamard", _ptrs(G), self.N, R, -1, sig.data_ptr(), sig.data_ptr(), None,
                   terms[1:2].data_ptr(), st)
         return terms
+
+    def _exact_mttkrp_dev(self, U_L, j: int, out, out_rows, stream) -> None:
+        R = int(U_L[0].shape[1])
+        _lib.call("ftl_sparse_exact_mttkrp", self.idx_dev.data_ptr(), self.vals_dev.data_ptr(), self.nnz, self.N, j,
+                  _ptrs(U_L), R, out, out_rows, stream)
 
     def execute_rrf(self, lr: "LowRankTensor", seed: int | None = None) -> None:
         """Randomized range-finder initialisation of `lr` (SparseTensor::

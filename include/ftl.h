@@ -284,6 +284,64 @@ int ftl_sparse_exact_mttkrp(const uint32_t *idx_dev, const double *vals_dev, int
 int ftl_sparse_rrf(const int32_t *row_idx, const uint64_t *row_keys, const double *row_vals, int64_t nnz,
                    int R, uint64_t seed, uint32_t mode, double *out, int64_t I_j, void *stream);
 
+/* ---- black-box right-hand sides (low-rank and dense tensors) --------------
+ * The sampled MTTKRP of ALS against a tensor that is not sparse
+ * (BlackBoxTensor::execute_downsampled_mttkrp, cpp_ext/black_box_tensor.hpp:21-67):
+ * out (rows 0..I_j-1) = sum over unique samples u of fiber_u (x) coef_u h[rep_u],
+ * coef_u = w[rep_u] * ucnt[u] (urep/ucnt/w NULL: u itself, 1, 1); rows
+ * I_j..out_rows-1 are zeroed.  samples is N x J (mode-major, as ftl_krp_draw
+ * writes them); num_unique comes from num_unique_dev when that is not NULL. */
+
+/* Low-rank tensor [[sigma_rhs; V]] (rank Rr): fiber = V_j (sigma o prod V_k[s_k])
+ * (LowRankTensor::materialize_rhs, cpp_ext/low_rank_tensor.hpp:91-135), computed
+ * as V_j (P^T L) without materialising fibers.  Deterministic. */
+int ftl_lowrank_mttkrp_workspace_bytes(int Rr, int R, size_t *out);
+int ftl_lowrank_sampled_mttkrp(const double *const *V, const double *sigma_rhs, int N, int Rr, int j,
+                               const uint64_t *samples, int64_t J, const int32_t *urep, const int32_t *ucnt,
+                               const int64_t *num_unique_dev, int64_t num_unique, const double *w,
+                               const double *h, int R, void *workspace, size_t ws_bytes, double *out,
+                               int64_t I_j, int64_t out_rows, void *stream);
+/* Dense row-major tensor (FP64 or FP32, dims[N]): fiber = T[s_0, .., :, .., s_N-1]
+ * (DenseTensor::materialize_rhs, cpp_ext/dense_tensor.hpp:38-59). */
+int ftl_dense_sampled_mttkrp(const void *T, int is_f32, const int64_t *dims, int N, int j,
+                             const uint64_t *samples, int64_t J, const int32_t *urep, const int32_t *ucnt,
+                             const int64_t *num_unique_dev, int64_t num_unique, const double *w,
+                             const double *h, int R, double *out, int64_t out_rows, void *stream);
+/* out (n x I_j) = the dense tensor's fibers at n samples (n x N, row-major). */
+int ftl_dense_materialize(const void *T, int is_f32, const int64_t *dims, int N, int j,
+                          const uint64_t *samples, int64_t n, double *out, void *stream);
+/* out[0] = sum over all entries of (T - [[sigma; U]])^2 (U NULL: model 0),
+ * out[1] = sum of T^2.  The reference's DenseTensor has no residual (its base
+ * class returns -1); this is an addition. */
+int ftl_dense_residual_workspace_bytes(size_t *out);
+int ftl_dense_residual_terms(const void *T, int is_f32, const int64_t *dims, int N, const double *const *U,
+                             const double *sigma, int R, void *workspace, size_t ws_bytes, double *out,
+                             void *stream);
+/* Low-rank tensor at n index tuples (n x N, uint32 or uint64, row-major):
+ * out[z] = sum_r sigma_r prod_k U_k[idx(z,k), r]
+ * (LowRankTensor::evaluate_indices, cpp_ext/low_rank_tensor.hpp:262-280). */
+int ftl_lowrank_evaluate(const double *const *U, int N, int R, const double *sigma, const void *idx,
+                         int idx_is_u64, int64_t n, double *out, void *stream);
+/* Fibers of a low-rank tensor at n samples (n x N uint64, row-major): j >= N:
+ * out (n x R) = sigma o prod_k U_k[s_k]; else out (n x I_j) = that row times
+ * U_j^T (LowRankTensor::materialize_rhs, cpp_ext/low_rank_tensor.hpp:91-135). */
+int ftl_lowrank_materialize(const double *const *U, int N, int R, const double *sigma, const uint64_t *samples,
+                            int64_t n, int j, int64_t I_j, double *out, void *stream);
+/* out (out_rows x C) = X (I x K) M (K x C) in rows 0..I-1, zeros below
+ * (the final product of LowRankTensor::execute_exact_mttkrp,
+ * cpp_ext/low_rank_tensor.hpp:147-180). */
+int ftl_rows_times(const double *X, int64_t I, int K, const double *M, int C, double *out, int64_t out_rows,
+                   void *stream);
+/* out (Ra x Rb) = A^T B over I rows (FP64, fixed-order two-stage reduction). */
+int ftl_cross_gram_workspace_bytes(int Ra, int Rb, size_t *out);
+int ftl_cross_gram(const double *A, int Ra, const double *B, int Rb, int64_t I, void *workspace,
+                   size_t ws_bytes, double *out, void *stream);
+/* M = (sigma_a sigma_b^T) o prod_{k != exclude} grams[k] (each Ra x Rb), and/or
+ * the sum of M's entries (ATB_chain_prod / ATB_chain_prod_sum,
+ * cpp_ext/common.h:152-226, rectangular). */
+int ftl_chain_prod(const double *const *grams, int N, int Ra, int Rb, int exclude, const double *sigma_a,
+                   const double *sigma_b, double *out_mat, double *out_sum, void *stream);
+
 /* out_mat (R x R) = (sigma_a sigma_b^T) o prod_{k != exclude} G_k over N full
  * R x R FP64 Grams (host array of device pointers; exclude = -1 for none; a
  * NULL sigma means all ones); out_sum = sum of its entries.  Either output

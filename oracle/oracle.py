@@ -296,17 +296,20 @@ class OracleALS:
     over OracleKRPSampler, for a COO sparse tensor (SortIdxLookup semantics,
     cpp_ext/sort_lookup.hpp:69-132)."""
 
-    def __init__(self, U_list, sigma, idx, vals, J: int, dims=None):
+    def __init__(self, U_list, sigma, idx, vals, J: int, dims=None, rhs=None):
         self.U = [np.array(u, dtype=np.float64, copy=True) for u in U_list]
         self.N = len(self.U)
         self.R = self.U[0].shape[1]
         self.sigma = np.array(sigma, dtype=np.float64, copy=True)
-        self.idx = np.ascontiguousarray(idx, dtype=np.uint32)
-        self.vals = np.asarray(vals, dtype=np.float64)
+        self.rhs = rhs          # a black-box right-hand side (OracleLowRankRHS / OracleDenseRHS)
         self.dims = list(dims) if dims is not None else [u.shape[0] for u in self.U]
         self.J = J
         self.sampler = OracleKRPSampler(self.U, J, self.R)
         self.lookups = []
+        if rhs is not None:
+            return
+        self.idx = np.ascontiguousarray(idx, dtype=np.uint32)
+        self.vals = np.asarray(vals, dtype=np.float64)
         for j in range(self.N):
             k = fiber_keys(self.idx, self.dims, j)
             perm = np.argsort(k, kind="stable")
@@ -324,6 +327,12 @@ class OracleALS:
         hd = h[first] * np.sqrt(wd)[:, None]                        # :155-160
         pinv = pinv_square(hd.T @ hd, min(len(uk), R), 1e-11)       # :164-165
         hd = hd * np.sqrt(wd)[:, None]                              # :169-174
+        if self.rhs is not None:                                    # black_box_tensor.hpp:21-67
+            out = np.zeros((self.U[j].shape[0], R))
+            fib = self.rhs.fibers(T[first], j)                      # unique samples x I_j
+            out[: fib.shape[1]] = fib.T @ hd
+            self.U[j] = out @ pinv
+            return self._finish_update(j, renormalize, update_sampler, samples)
         skeys, sidx, svals = self.lookups[j]
         lo = np.searchsorted(skeys, uk, side="left")
         hi = np.searchsorted(skeys, uk, side="right")
@@ -332,6 +341,9 @@ class OracleALS:
             for z in range(lo[u], hi[u]):
                 out[sidx[z]] += svals[z] * hd[u]
         self.U[j] = out @ pinv                                      # :189-203
+        return self._finish_update(j, renormalize, update_sampler, samples)
+
+    def _finish_update(self, j, renormalize, update_sampler, samples):
         if renormalize:                                             # low_rank_tensor.hpp:203-260
             norms = np.sqrt((self.U[j] ** 2).sum(axis=0))
             norms[norms <= 1e-7] = 1.0
@@ -388,3 +400,51 @@ def rrf(idx: np.ndarray, vals: np.ndarray, dims, rows, R: int, seed: int) -> lis
             U[idx[z, j]] += vals[z] * cache[k]
         out.append(U)
     return out
+
+
+class OracleLowRankRHS:
+    """A low-rank right-hand side [[sigma; V]] (LowRankTensor as a
+    BlackBoxTensor, low_rank_tensor.hpp:91-135): the fiber of sample s along
+    mode j is V_j (sigma o prod_{k != j} V_k[s_k])."""
+
+    def __init__(self, V, sigma):
+        self.V = [np.asarray(v, dtype=np.float64) for v in V]
+        self.sigma = np.asarray(sigma, dtype=np.float64)
+
+    def partial(self, S, j):
+        P = np.ones((S.shape[0], self.sigma.size)) * self.sigma[None, :]
+        for k, v in enumerate(self.V):
+            if k != j:
+                P = P * v[S[:, k]]
+        return P
+
+    def fibers(self, S, j):
+        return self.partial(S, j) @ self.V[j].T
+
+    def evaluate(self, idx):
+        return self.partial(np.asarray(idx, dtype=np.int64), -1).sum(axis=1)
+
+    def residual_normsq(self, sigma, U):
+        """||[[sigma; U]] - [[s; V]]||^2 by Gram chains (low_rank_tensor.hpp:78-89)."""
+        def chain(A, sa, B, sb):
+            G = np.outer(sa, sb)
+            for a, b in zip(A, B):
+                G = G * (a.T @ b)
+            return G.sum()
+        return max(chain(self.V, self.sigma, self.V, self.sigma) + chain(U, sigma, U, sigma)
+                   - 2 * chain(U, sigma, self.V, self.sigma), 0.0)
+
+
+class OracleDenseRHS:
+    """A dense right-hand side (DenseTensor, dense_tensor.hpp:38-59): the
+    fiber of sample s along mode j is T[s_0, .., :, .., s_{N-1}]."""
+
+    def __init__(self, T):
+        self.T = np.asarray(T, dtype=np.float64)
+
+    def fibers(self, S, j):
+        N = self.T.ndim
+        out = np.empty((S.shape[0], self.T.shape[j]))
+        for i in range(S.shape[0]):
+            out[i] = self.T[tuple(S[i, k] if k != j else slice(None) for k in range(N))]
+        return out

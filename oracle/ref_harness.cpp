@@ -170,6 +170,8 @@ PYBIND11_MODULE(ftl_ref, m) {
         .def("renormalize_columns", &LowRankTensor::renormalize_columns)
         .def("materialize_rhs", &LowRankTensor::materialize_rhs_py)
         .def("evaluate_indices", &LowRankTensor::evaluate_indices_py);
+    py::class_<DenseTensor<double>, BlackBoxTensor>(m, "DenseTensor", py::module_local())
+        .def(py::init<py::array_t<double>, uint64_t>());
     py::class_<SparseTensor, Tensor>(m, "SparseTensor", py::module_local())
         .def(py::init<py::array_t<uint32_t>, py::array_t<double>, std::string>())
         .def("execute_rrf", &SparseTensor::execute_rrf);

@@ -47,3 +47,19 @@ def load_als(name):
                          sigma=z[f"sigma_{u}"]) for u in range(n_upd)]
     c["resid"] = [float(z[f"resid_{s}"]) for s in range(c["sweeps"])]
     return c
+
+
+def bb_cases():
+    return sorted(p.stem for p in GOLDEN.glob("bb_*.npz"))
+
+
+def load_bb(name):
+    z = np.load(GOLDEN / f"{name}.npz")
+    dims = [int(d) for d in z["dims"]]
+    N = len(dims)
+    c = {k: z[k] for k in z.files}
+    c.update(kind=str(z["kind"]), dims=dims, N=N, R=int(z["R"]), Rr=int(z["Rr"]), J=int(z["J"]),
+             sweeps=int(z["sweeps"]), V=[z[f"V_{k}"] for k in range(N)], U0=[z[f"U0_{k}"] for k in range(N)])
+    c["updates"] = [dict(j=u % N, draws=z[f"draws_{u}"], samples=z[f"samples_{u}"], U=z[f"U_{u}"],
+                         sigma=z[f"sigma_{u}"]) for u in range(c["sweeps"] * N)]
+    return c

@@ -6,7 +6,7 @@ from its sources by `make -C oracle ref` into oracle/_ref/ftl_ref*.so, on
 seeded inputs with injected uniforms, and stores inputs, uniforms and the
 reference's outputs (sample indices, h, weights, node Grams).
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [--only bb]
 """
 from __future__ import annotations
 
@@ -100,7 +100,85 @@ def make_als_case(name, dims, nnz, R, J, sweeps, seed):
     print(name, "written")
 
 
+# name: (kind, dims, rhs rank, R, J, sweeps, seed)
+BB_CASES = {
+    "bb_lowrank_4mode_r6": ("lowrank", [30, 22, 18, 25], 4, 6, 500, 2, 41),
+    "bb_dense_3mode_r5": ("dense", [16, 13, 11], 3, 5, 400, 2, 42),
+}
+
+
+def make_blackbox_case(name, kind, dims, Rr, R, J, sweeps, seed):
+    """Reference ALS against a black-box right-hand side (BlackBoxTensor::
+    execute_downsampled_mttkrp, cpp_ext/black_box_tensor.hpp:21-67): a
+    low-rank tensor (LowRankTensor(Rr, 10000, V)) or a dense one
+    (DenseTensor<double>: rank-Rr tensor plus 10% Gaussian noise), injected
+    uniforms, every update's samples and factor; for the low-rank case also
+    the residual after each sweep and materialize_rhs / evaluate_indices
+    vectors."""
+    rng = np.random.default_rng(seed)
+    N = len(dims)
+    V = [rng.normal(size=(d, Rr)) for d in dims]
+    out = {f"V_{k}": V[k] for k in range(N)}
+    if kind == "lowrank":
+        rhs = ftl_ref.LowRankTensor(Rr, 10000, V)
+        sv = np.zeros(Rr)
+        rhs.get_sigma(sv, -1)
+        out["sv"] = sv
+        out["normsq_rhs"] = np.array(rhs.get_normsq())
+        S = np.stack([rng.integers(0, d, size=60) for d in dims], axis=1).astype(np.uint64)
+        out["mat_S"] = S
+        for jj in (1, N):
+            m = np.zeros((60, dims[jj] if jj < N else Rr))
+            rhs.materialize_rhs(S, jj, m)
+            out[f"mat_{jj}"] = m
+        ev = np.zeros(60)
+        rhs.evaluate_indices(S.astype(np.uint32), ev)
+        out["eval"] = ev
+    else:
+        T = np.einsum("ir,jr,kr->ijk", *V) + 0.1 * rng.normal(size=dims)
+        T = np.ascontiguousarray(T)
+        rhs = ftl_ref.DenseTensor(T, 10000)
+        out["T"] = T
+    U = [rng.normal(size=(d, R)) for d in dims]
+    lr = ftl_ref.LowRankTensor(R, U)
+    lr.renormalize_columns(-1)
+    sigma0 = np.zeros(R)
+    lr.get_sigma(sigma0, -1)
+    out.update({f"U0_{k}": U[k].copy() for k in range(N)})
+    als = ftl_ref.InjectedALS(lr, rhs)
+    als.initialize_ds_als(J)
+    upd = 0
+    for sw in range(sweeps):
+        for j in range(N):
+            d = rng.random(2 * N * J)
+            als.set_draws(d)
+            als.execute_ds_als_update(j, True, True)
+            smp = np.zeros((N, J), dtype=np.uint64)
+            als.get_samples(smp)
+            sg = np.zeros(R)
+            lr.get_sigma(sg, -1)
+            out[f"draws_{upd}"] = d
+            out[f"samples_{upd}"] = smp
+            out[f"U_{upd}"] = U[j].copy()
+            out[f"sigma_{upd}"] = sg
+            upd += 1
+        if kind == "lowrank":
+            sg = np.zeros(R)
+            lr.get_sigma(sg, -1)
+            out[f"resid_{sw}"] = np.array(rhs.compute_residual_normsq(sg, U))
+    out.update(kind=kind, dims=np.array(dims), Rr=Rr, R=R, J=J, sweeps=sweeps, sigma0=sigma0)
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "written")
+
+
 def main() -> None:
+    if "--only" in sys.argv:
+        which = sys.argv[sys.argv.index("--only") + 1]
+        if which == "bb":
+            for name, args in BB_CASES.items():
+                make_blackbox_case(name, *args)
+            return
+        raise SystemExit(f"unknown --only {which}")
     for name, (N, dims, R, J, j, seed, heavy) in KRP_CASES.items():
         rng = np.random.default_rng(seed)
         U = make_factors(rng, dims, R, heavy)
@@ -118,6 +196,8 @@ def main() -> None:
         print(name, "written")
     for name, args in ALS_CASES.items():
         make_als_case(name, *args)
+    for name, args in BB_CASES.items():
+        make_blackbox_case(name, *args)
     for name, (n, F, R, J, seed) in TREE_CASES.items():
         rng = np.random.default_rng(seed)
         U = rng.normal(size=(n, R))

@@ -232,3 +232,100 @@ def test_gpu_rrf_matches_oracle_and_is_gaussian(ftl):
     assert np.abs(corr - np.eye(8)).max() < 0.05
     ref = np.stack([O.fiber_normals(5, 0, int(k), R2) for k in rkeys[:50].cpu().numpy()])
     np.testing.assert_allclose(g[rrows[:50].cpu().numpy()], ref, rtol=0, atol=1e-5)
+
+
+from tests._golden import bb_cases, load_bb  # noqa: E402
+
+
+def _bb_rhs(ftl, c, f32=False):
+    if c["kind"] == "lowrank":
+        V = [v.copy() for v in c["V"]]
+        t = ftl.LowRankTensor(c["Rr"], 10000, V)
+        t.set_sigma(c["sv"])
+        return t
+    return ftl.DenseTensor(c["T"].astype(np.float32) if f32 else c["T"], 10000)
+
+
+@pytest.mark.parametrize("name", bb_cases())
+def test_gpu_blackbox_als_matches_reference_golden(ftl, name):
+    """CP-ALS against a low-rank / dense right-hand side (black_box_tensor.hpp:
+    21-67) vs the reference with the same uniforms: samples identical,
+    factors within 1e-9 of the largest entry, sigma 1e-9 relative, and for
+    the low-rank case the residual 1e-9 and the fit 1e-6 relative."""
+    c = load_bb(name)
+    rhs = _bb_rhs(ftl, c)
+    U = [u.copy() for u in c["U0"]]
+    lr = ftl.LowRankTensor(c["R"], U)
+    lr.set_sigma(c["sigma0"])
+    als = ftl.ALS(lr, rhs)
+    als.initialize_ds_als(c["J"], "efficient", precision="fp64")
+    N = c["N"]
+    for u, upd in enumerate(c["updates"]):
+        j = upd["j"]
+        als.execute_ds_als_update(j, True, True, draws=upd["draws"])
+        samples = als.sampler.samples_dev.cpu().numpy().view(np.uint64)
+        rows = [k for k in range(N) if k != j]
+        assert np.array_equal(samples[rows], upd["samples"][rows]), f"update {u}"
+        np.testing.assert_allclose(U[j], upd["U"], rtol=0, atol=1e-9 * np.abs(upd["U"]).max())
+        np.testing.assert_allclose(lr.sigma, upd["sigma"], rtol=1e-9)
+        if c["kind"] == "lowrank" and (u + 1) % N == 0:
+            resid, ref = rhs.compute_residual_normsq(lr.sigma, U), float(c[f"resid_{u // N}"])
+            np.testing.assert_allclose(resid, ref, rtol=1e-9)
+            nrm = float(c["normsq_rhs"])
+            fit, fit_ref = 1 - np.sqrt(resid / nrm), 1 - np.sqrt(ref / nrm)
+            assert abs(fit - fit_ref) <= 1e-6 * abs(fit_ref)
+    if c["kind"] == "lowrank":
+        S = c["mat_S"]
+        for jj in (1, N):
+            m = np.zeros_like(c[f"mat_{jj}"])
+            rhs.materialize_rhs(S, jj, m)
+            np.testing.assert_allclose(m, c[f"mat_{jj}"], rtol=1e-12, atol=1e-12)
+        ev = np.zeros(S.shape[0])
+        rhs.evaluate_indices(S.astype(np.uint32), ev)
+        np.testing.assert_allclose(ev, c["eval"], rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(rhs.get_normsq(), float(c["normsq_rhs"]), rtol=1e-12)
+
+
+@pytest.mark.parametrize("name", bb_cases())
+def test_gpu_blackbox_downsampled_mttkrp_and_exact_update(ftl, name):
+    """Tensor-API MTTKRP (execute_downsampled_mttkrp_py) vs explicit fibers,
+    the FP32 dense tensor vs FP64, the dense residual, and (low-rank) the
+    exact ALS update vs its numpy statement (low_rank_tensor.hpp:147-180)."""
+    c = load_bb(name)
+    rng = np.random.default_rng(2)
+    rhs = _bb_rhs(ftl, c)
+    o = O.OracleLowRankRHS(c["V"], c["sv"]) if c["kind"] == "lowrank" else O.OracleDenseRHS(c["T"])
+    J, R, j = 700, 7, 1
+    S = np.stack([rng.integers(0, d, size=J) for d in c["dims"]], axis=1).astype(np.uint64)
+    L = rng.normal(size=(J, R))
+    out = np.zeros((c["dims"][j], R))
+    rhs.execute_downsampled_mttkrp_py(S, L, j, out)
+    want = o.fibers(S.astype(np.int64), j).T @ L
+    np.testing.assert_allclose(out, want, rtol=0, atol=1e-11 * np.abs(want).max())
+    if c["kind"] == "dense":
+        r32 = _bb_rhs(ftl, c, f32=True)
+        o32 = np.zeros_like(out)
+        r32.execute_downsampled_mttkrp_py(S, L, j, o32)
+        np.testing.assert_allclose(o32, want, rtol=0, atol=1e-5 * np.abs(want).max())
+        Ul = [rng.normal(size=(d, 3)) for d in c["dims"]]
+        sg = rng.random(3) + 0.5
+        model = np.einsum("r,ir,jr,kr->ijk", sg, *Ul)
+        np.testing.assert_allclose(rhs.compute_residual_normsq(sg, Ul), ((c["T"] - model) ** 2).sum(), rtol=1e-11)
+        np.testing.assert_allclose(rhs.get_normsq(), (c["T"] ** 2).sum(), rtol=1e-12)
+        return
+    Rl = 5
+    U = [rng.normal(size=(d, Rl)) for d in c["dims"]]
+    Uo = [u.copy() for u in U]
+    lr = ftl.LowRankTensor(Rl, U)
+    als = ftl.ALS(lr, rhs)
+    als.execute_exact_als_update(j, True, False)
+    G = np.ones((Rl, Rl))
+    M = np.outer(c["sv"], np.ones(Rl))
+    for k in range(c["N"]):
+        if k != j:
+            G = G * (Uo[k].T @ Uo[k])
+            M = M * (c["V"][k].T @ Uo[k])
+    mt = c["V"][j] @ M
+    Uj = mt @ O.pinv_square(G, Rl, 1e-11)
+    n = np.linalg.norm(Uj, axis=0)
+    np.testing.assert_allclose(U[j], Uj / n, rtol=0, atol=1e-9 * np.abs(Uj / n).max())

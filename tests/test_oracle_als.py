@@ -118,3 +118,92 @@ def test_fiber_normals_are_standard_normal():
     g = np.concatenate([O.fiber_normals(9, 1, k * 7919 + 3, 64) for k in range(400)])
     assert abs(g.mean()) < 0.02 and abs(g.var() - 1.0) < 0.03
     assert abs(((g - g.mean()) ** 4).mean() / g.var() ** 2 - 3.0) < 0.15
+
+
+def _ref_module():
+    ref_dir = REPO / "oracle" / "_ref"
+    if not list(ref_dir.glob("ftl_ref*.so")):
+        pytest.skip("reference module not built (make -C oracle ref)")
+    sys.path.insert(0, str(ref_dir))
+    import ftl_ref
+    return ftl_ref
+
+
+@pytest.mark.parametrize("kind", ["lowrank", "dense"])
+def test_oracle_blackbox_als_matches_live_reference(kind):
+    """ALS against a black-box right-hand side (BlackBoxTensor::
+    execute_downsampled_mttkrp, black_box_tensor.hpp:21-67): a low-rank
+    tensor (low_rank_tensor.hpp:91-135) or a dense one (dense_tensor.hpp:
+    38-59), with injected uniforms, oracle vs the reference."""
+    ftl_ref = _ref_module()
+    rng = np.random.default_rng(31 if kind == "lowrank" else 32)
+    dims, N, R, J = [14, 11, 9], 3, 5, 300
+    V = [rng.normal(size=(d, 3)) for d in dims]
+    if kind == "lowrank":
+        rhs_ref = ftl_ref.LowRankTensor(3, 10000, V)
+        sv = np.zeros(3)
+        rhs_ref.get_sigma(sv, -1)
+        rhs = O.OracleLowRankRHS(V, sv)
+    else:
+        T = np.einsum("ir,jr,kr->ijk", *V) + 0.1 * rng.normal(size=dims)
+        rhs_ref = ftl_ref.DenseTensor(np.ascontiguousarray(T), 10000)
+        rhs = O.OracleDenseRHS(T)
+    U = [rng.normal(size=(d, R)) for d in dims]
+    lr = ftl_ref.LowRankTensor(R, U)
+    lr.renormalize_columns(-1)
+    sig = np.zeros(R)
+    lr.get_sigma(sig, -1)
+    o = O.OracleALS([u.copy() for u in U], sig, None, None, J, dims, rhs=rhs)
+    als = ftl_ref.InjectedALS(lr, rhs_ref)
+    als.initialize_ds_als(J)
+    for j in [0, 1, 2, 0, 1, 2]:
+        d = rng.random(2 * N * J)
+        als.set_draws(d)
+        als.execute_ds_als_update(j, True, True)
+        o.update(j, d)
+        np.testing.assert_allclose(o.U[j], U[j], rtol=0, atol=1e-11 * np.abs(U[j]).max())
+    if kind == "lowrank":
+        s2 = np.zeros(R)
+        lr.get_sigma(s2, -1)
+        np.testing.assert_allclose(rhs.residual_normsq(s2, U), rhs_ref.compute_residual_normsq(s2, U), rtol=1e-10)
+
+
+def test_oracle_lowrank_materialize_and_evaluate_match_reference():
+    ftl_ref = _ref_module()
+    rng = np.random.default_rng(8)
+    dims, R = [20, 15, 12, 9], 4
+    V = [rng.normal(size=(d, R)) for d in dims]
+    t = ftl_ref.LowRankTensor(R, 10000, V)
+    sv = np.zeros(R)
+    t.get_sigma(sv, -1)
+    o = O.OracleLowRankRHS(V, sv)
+    S = np.stack([rng.integers(0, d, size=40) for d in dims], axis=1).astype(np.uint64)
+    for j in (1, 4):
+        out = np.zeros((40, dims[j] if j < 4 else R))
+        t.materialize_rhs(S, j, out)
+        want = o.fibers(S.astype(np.int64), j) if j < 4 else o.partial(S.astype(np.int64), -1)
+        np.testing.assert_allclose(out, want, rtol=1e-12, atol=1e-12)
+    idx = S.astype(np.uint32)
+    res = np.zeros(40)
+    t.evaluate_indices(idx, res)
+    np.testing.assert_allclose(res, o.evaluate(idx), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", __import__("tests._golden", fromlist=["bb_cases"]).bb_cases())
+def test_oracle_blackbox_als_matches_golden(name):
+    from tests._golden import load_bb
+    c = load_bb(name)
+    rhs = O.OracleLowRankRHS(c["V"], c["sv"]) if c["kind"] == "lowrank" else O.OracleDenseRHS(c["T"])
+    o = O.OracleALS(c["U0"], c["sigma0"], None, None, c["J"], c["dims"], rhs=rhs)
+    for u, upd in enumerate(c["updates"]):
+        o.update(upd["j"], upd["draws"])
+        rows = [k for k in range(c["N"]) if k != upd["j"]]
+        assert np.array_equal(o.last_samples[rows], upd["samples"][rows])
+        np.testing.assert_allclose(o.U[upd["j"]], upd["U"], rtol=0, atol=1e-11 * np.abs(upd["U"]).max())
+        np.testing.assert_allclose(o.sigma, upd["sigma"], rtol=1e-11)
+        if c["kind"] == "lowrank" and (u + 1) % c["N"] == 0:
+            np.testing.assert_allclose(rhs.residual_normsq(o.sigma, o.U), c[f"resid_{u // c['N']}"], rtol=1e-10)
+    if c["kind"] == "lowrank":
+        S = c["mat_S"].astype(np.int64)
+        np.testing.assert_allclose(rhs.fibers(S, 1), c["mat_1"], rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(rhs.evaluate(S), c["eval"], rtol=1e-12, atol=1e-12)
