@@ -65,7 +65,7 @@ class ALS:
         # no FP32 factor copies: every update rebuilds one tree, and a copy pass
         # over a (mostly zero) factor would cost more than the leaf scans save
         self.sampler = Sampler(lr.U_dev, self.J, lr.R, "efficient", precision=precision, seed=seed,
-                               device=self.device, factor_shadows=False)
+                               device=self.device, factor_shadows=False, overlap_computem=False)
         assert all(a.data_ptr() == b.data_ptr() for a, b in zip(self.sampler.U, lr.U_dev))
         dev, R, J = self.device, lr.R, self.J
         self._keys = torch.empty(J, dtype=torch.int64, device=dev)

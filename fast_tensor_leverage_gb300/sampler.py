@@ -22,7 +22,8 @@ from . import _lib
 
 class Sampler:
     def __init__(self, U, J: int, R: int, type: str = "efficient", *, precision: str = "fp64",
-                 seed: int | None = None, device=None, factor_shadows: bool = True):
+                 seed: int | None = None, device=None, factor_shadows: bool = True,
+                 overlap_computem: bool = True):
         if type != "efficient":
             raise ValueError(
                 f"Unsupported argument {type!r} passed for sampler construction "
@@ -58,17 +59,34 @@ class Sampler:
             nb = _lib.tree_bytes(self.dims[k], self.F[k], R, self._prec)
             self.trees.append(torch.empty(nb // tdt.itemsize, dtype=tdt, device=dev))
         eig_b, M_b, lam_b, p32_b = _lib.plan_sizes(N, R, self._prec)
-        self.eig_G = torch.empty(eig_b // tdt.itemsize, dtype=tdt, device=dev)
-        self.M = torch.zeros(M_b // 8, dtype=torch.float64, device=dev)
-        self.lam = torch.zeros(lam_b // 8, dtype=torch.float64, device=dev)
-        self.pinv32 = torch.zeros(p32_b // 4, dtype=torch.float32, device=dev)
+        # Per-draw workspaces (eigen trees, computeM matrices).  With
+        # overlap_computem there are two sets: computeM of the next draw runs
+        # on a side stream into the other set while the current descent runs
+        # (computeM is a few single-CTA kernels that would otherwise leave the
+        # GPU idle between descents).  Every draw still does all its work.
+        self._ws_sets = []
+        for _ in range(2 if overlap_computem else 1):
+            self._ws_sets.append((torch.empty(eig_b // tdt.itemsize, dtype=tdt, device=dev),
+                                  torch.zeros(M_b // 8, dtype=torch.float64, device=dev),
+                                  torch.zeros(lam_b // 8, dtype=torch.float64, device=dev),
+                                  torch.zeros(p32_b // 4, dtype=torch.float32, device=dev)))
+        self.eig_G, self.M, self.lam, self.pinv32 = self._ws_sets[0]
         self.samples_dev = torch.zeros((N, J), dtype=torch.int64, device=dev)
         self.h_dev = torch.empty((J, R), dtype=torch.float64, device=dev)
         self.weights_dev = torch.empty(J, dtype=torch.float64, device=dev)
         self.seed = int(seed) if seed is not None else secrets.randbits(63)
         self.counter = 0
-        self._stage = D.PinnedStage()
-        self._plan = _lib.KRPPlan()
+        self._overlap = overlap_computem
+        self._plans = [_lib.KRPPlan() for _ in self._ws_sets]
+        self._plan = self._plans[0]        # the plan of the last draw
+        self._next_set = 0
+        if overlap_computem:
+            # high priority: the computeM CTAs are dispatched ahead of the
+            # queued blocks of the running descent as soon as an SM frees up
+            self._cm_stream = torch.cuda.Stream(dev, priority=-1)
+            self._cm_done = [torch.cuda.Event() for _ in self._ws_sets]
+            self._set_free = [None] * len(self._ws_sets)
+        self._tree_ev = torch.cuda.Event()
         self._refresh_plan()
         for k in range(N):
             self.update_sampler(k)
@@ -84,17 +102,17 @@ class Sampler:
 
     # ----------------------------------------------------------- plumbing
     def _refresh_plan(self) -> None:
-        p = self._plan
-        p.N, p.R, p.J, p.prec = self.N, self.R, self.J, self._prec
-        for k in range(self.N):
-            p.dims[k] = self.dims[k]
-            p.U[k] = self.U[k].data_ptr()
-            p.U32[k] = self.U32[k].data_ptr() if self.U32 is not None else None
-            p.gram_G[k] = self.trees[k].data_ptr()
-        p.eig_G = self.eig_G.data_ptr()
-        p.M = self.M.data_ptr()
-        p.lambda_ = self.lam.data_ptr()
-        p.pinv32 = self.pinv32.data_ptr()
+        for p, (eig, M, lam, p32) in zip(self._plans, self._ws_sets):
+            p.N, p.R, p.J, p.prec = self.N, self.R, self.J, self._prec
+            for k in range(self.N):
+                p.dims[k] = self.dims[k]
+                p.U[k] = self.U[k].data_ptr()
+                p.U32[k] = self.U32[k].data_ptr() if self.U32 is not None else None
+                p.gram_G[k] = self.trees[k].data_ptr()
+            p.eig_G = eig.data_ptr()
+            p.M = M.data_ptr()
+            p.lambda_ = lam.data_ptr()
+            p.pinv32 = p32.data_ptr()
 
     def _stream(self, stream=None) -> int:
         return D.stream_ptr(self.device, stream)
@@ -108,6 +126,8 @@ class Sampler:
         if self.U32 is not None:
             _lib.call("ftl_factor_shadow", self.U[j].data_ptr(), self.dims[j] * self.R, self.U32[j].data_ptr(),
                       self._stream(stream))
+        # computeM on the side stream must see this tree
+        self._tree_ev.record(stream if stream is not None else torch.cuda.current_stream(self.device))
 
     def set_factor(self, j: int, U, stream=None) -> None:
         """Replace factor j (same shape) and rebuild its tree."""
@@ -126,25 +146,53 @@ class Sampler:
         device tensors (samples N x J int64 holding the uint64 row indices,
         h J x R, weights J); they are overwritten by the next draw.
         `draws` (2N x J uniforms, the reference's layout; numpy or CUDA
-        tensor) replaces the in-kernel Philox stream."""
+        tensor, or a pinned CPU tensor, copied without blocking) replaces the
+        in-kernel Philox stream."""
         j = int(j)
         if j < 0:
             raise ValueError(f"j={j} must be non-negative")
+        main = stream if stream is not None else torch.cuda.current_stream(self.device)
+        plan = self._plan
+        if self._overlap:
+            b = self._next_set
+            self._next_set = (b + 1) % len(self._plans)
+            plan, cm = self._plans[b], self._cm_stream
+            # computeM(b) after the trees it reads and after the descent that
+            # last read workspace set b (it does not need the uniforms, so it
+            # is launched before they are copied); the descent after it
+            cm.wait_event(self._tree_ev)
+            if self._set_free[b] is not None:
+                cm.wait_event(self._set_free[b])
+            _lib.call("ftl_krp_compute_m", ctypes.byref(plan), j, int(cm.cuda_stream))
+            self._cm_done[b].record(cm)
         d_ptr = None
         if draws is not None:
             n = 2 * self.N * self.J
-            if isinstance(draws, torch.Tensor):
-                dt = draws.to(self.device, torch.float64).reshape(-1).contiguous()
-            else:
-                dt = torch.from_numpy(np.ascontiguousarray(np.asarray(draws, dtype=np.float64)).reshape(-1))
-                dt = dt.to(self.device, non_blocking=False)
+            with torch.cuda.stream(main):
+                if isinstance(draws, torch.Tensor):
+                    dt = draws.to(self.device, torch.float64, non_blocking=draws.is_pinned()).reshape(-1)
+                    dt = dt.contiguous()
+                else:
+                    dt = torch.from_numpy(np.ascontiguousarray(np.asarray(draws, dtype=np.float64)).reshape(-1))
+                    dt = dt.to(self.device, non_blocking=False)
             if dt.numel() != n:
                 raise ValueError(f"draws must hold 2*N*J = {n} uniforms, got {dt.numel()}")
             self._draws_keep = dt
             d_ptr = dt.data_ptr()
-        _lib.call("ftl_krp_draw", ctypes.byref(self._plan), j, self.samples_dev.data_ptr(),
-                  self.h_dev.data_ptr(), self.weights_dev.data_ptr(), d_ptr, self.seed,
-                  self.counter, self._stream(stream))
+        if self._overlap:
+            main.wait_event(self._cm_done[b])
+            _lib.call("ftl_krp_sample", ctypes.byref(plan), j, self.samples_dev.data_ptr(),
+                      self.h_dev.data_ptr(), self.weights_dev.data_ptr(), d_ptr, self.seed,
+                      self.counter, int(main.cuda_stream))
+            ev = torch.cuda.Event()
+            ev.record(main)
+            self._set_free[b] = ev
+            self._plan = plan
+            self.eig_G, self.M, self.lam, self.pinv32 = self._ws_sets[b]
+        else:
+            _lib.call("ftl_krp_draw", ctypes.byref(plan), j, self.samples_dev.data_ptr(),
+                      self.h_dev.data_ptr(), self.weights_dev.data_ptr(), d_ptr, self.seed,
+                      self.counter, int(main.cuda_stream))
         if d_ptr is None:
             self.counter += 2 * self.N * self.J
         return self.samples_dev, self.h_dev, self.weights_dev
@@ -152,19 +200,23 @@ class Sampler:
     def _rows(self, j: int):
         return [k for k in range(self.N) if k != j]
 
+    def _copy_rows_out(self, j: int, s_out) -> None:
+        # straight from the device into the caller's array (one copy; rows of
+        # excluded modes are left as they are, as in the reference)
+        N, J = self.N, self.J
+        flat = s_out.reshape(-1)[: N * J].reshape(N, J).view(np.int64)
+        if j >= N:
+            torch.from_numpy(flat).copy_(self.samples_dev)
+        else:
+            for k in self._rows(j):
+                torch.from_numpy(flat[k]).copy_(self.samples_dev[k])
+
     def KRPDrawSamples(self, j: int, samples, draws=None) -> None:
         """Draw J samples from the KRP of all factors except j into
         samples (N x J uint64, row j untouched when j < N), in place."""
-        N, J = self.N, self.J
-        s_out = D.require_numpy_out(samples, np.uint64, "samples", min_size=N * J)
+        s_out = D.require_numpy_out(samples, np.uint64, "samples", min_size=self.N * self.J)
         self.draw(j, draws)
-        stage = self._stage.get((N, J), torch.int64)
-        stage.copy_(self.samples_dev, non_blocking=True)
-        torch.cuda.current_stream(self.device).synchronize()
-        flat = s_out.reshape(-1)[: N * J].reshape(N, J)
-        host = stage.numpy().view(np.uint64)
-        for k in self._rows(j):
-            flat[k] = host[k]
+        self._copy_rows_out(int(j), s_out)
 
     def KRPDrawSamples_materialize(self, j: int, samples, h_out, weights_out, draws=None) -> None:
         """KRPDrawSamples plus copies of the sampled KRP rows h (J x R) and the
@@ -174,19 +226,9 @@ class Sampler:
         h_np = D.require_numpy_out(h_out, np.float64, "h_out", min_size=J * R)
         w_np = D.require_numpy_out(weights_out, np.float64, "weights_out", min_size=J)
         self.draw(j, draws)
-        s_st = self._stage.get((N, J), torch.int64)
-        h_st = self._stage.get((J, R), torch.float64)
-        w_st = self._stage.get((J,), torch.float64)
-        s_st.copy_(self.samples_dev, non_blocking=True)
-        h_st.copy_(self.h_dev, non_blocking=True)
-        w_st.copy_(self.weights_dev, non_blocking=True)
-        torch.cuda.current_stream(self.device).synchronize()
-        flat = s_out.reshape(-1)[: N * J].reshape(N, J)
-        host = s_st.numpy().view(np.uint64)
-        for k in self._rows(j):
-            flat[k] = host[k]
-        h_np.reshape(-1)[: J * R] = h_st.numpy().reshape(-1)
-        w_np.reshape(-1)[:J] = w_st.numpy()
+        self._copy_rows_out(int(j), s_out)
+        torch.from_numpy(h_np.reshape(-1)[: J * R]).copy_(self.h_dev.reshape(-1))
+        torch.from_numpy(w_np.reshape(-1)[:J]).copy_(self.weights_dev)
 
     # ------------------------------------------------------- inspection
     @property

@@ -273,7 +273,7 @@ class ServingEngine:
                 if isinstance(factors, GaussianFactors):
                     factors = factors.materialize(self.device)
                 s = Sampler(factors, req.J, _factor_shapes(factors)[1], "efficient",
-                            precision=req.precision, seed=req.seed, device=self.device)
+                            precision=req.precision, seed=req.seed, device=self.device, overlap_computem=False)
                 _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), min(req.j, 1 << 31), int(st.cuda_stream))
                 h._obj = s
                 h._event = torch.cuda.Event()
