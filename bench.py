@@ -338,7 +338,9 @@ def run_ours(args, ws, rank, local):
                        (2 * (I // R) - 1) * (R * (R + 1) // 2) * prec_bytes / 1e9),
                    "parallelism": f"replicas x{ws}"},
         "e2e": e2e,
-        "gpu_launches": 3 * args.steps,
+        # per draw: computem_pinv_kernel, computem_eig_kernel, krp_draw_kernel,
+        # krp_fixup_kernel (FP32; FP64 draws have no fix-up pass)
+        "gpu_launches": (4 if args.precision == "fp32" else 3) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "krp_draw_kernel", "kernel_ms": kernel_ms,
