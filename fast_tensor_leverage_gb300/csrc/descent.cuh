@@ -360,26 +360,31 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
     double t0 = draw * (double)mP;
     float th = (float)t0;
     float tl = (float)(t0 - (double)th);
-    int64_t steps = g.lfill_level + 1;
-    for (int64_t lvl = 0; lvl < steps; ++lvl) {
-        if (lvl == g.lfill_level && is_leaf(g, c)) break;
+    // 32-bit node index and level counter (node counts are far below 2^31:
+    // a tree is at most 2 I / F nodes)
+    const uint32_t ncount = (uint32_t)g.node_count;
+    const int lf = (int)g.lfill_level;
+    uint32_t cu = 0;
+    for (int lvl = 0; lvl <= lf; ++lvl) {
+        if (lvl == lf && 2u * cu + 1u >= ncount) break;
         float mL;
         if (lvl == 0) {
             mL = mL0;
         } else {
-            prefetch_next(G, S, g, c, U, R, lane);
-            mL = qf.eval(G + (2 * c + 1) * (int64_t)S, lane);
+            prefetch_next(G, S, g, (int64_t)cu, U, R, lane);
+            mL = qf.eval(G + (size_t)(2u * cu + 1u) * (size_t)S, lane);
         }
         bool left = ((th - mL) + tl) <= 0.0f;
         if (left) {
-            c = 2 * c + 1;
+            cu = 2u * cu + 1u;
             mP = mL;
         } else {
-            c = 2 * c + 2;
+            cu = 2u * cu + 2u;
             df_sub(th, tl, mL);
             mP = fmaxf(mP - mL, 0.0f);
         }
     }
+    c = (int64_t)cu;
     float f = mP > 0.0f ? (th + tl) / mP : 0.0f;
     frac = fminf(fmaxf(f, 0.0f), 1.0f);
     return c;
@@ -525,20 +530,51 @@ __device__ __forceinline__ int64_t leaf_scan(const UT *__restrict__ U, int R, co
     // prefix (rows >= 32 in the further slots).
     constexpr int FQ = Shape<RMAX>::FQ;
     T incl[FQ];
+    T tot;
+    if (sizeof(T) == 8) {
+        // FP64: the reference's sequential running sum (same association)
 #pragma unroll
-    for (int qi = 0; qi < FQ; ++qi) incl[qi] = T(0);
-    T run = T(0);
+        for (int qi = 0; qi < FQ; ++qi) incl[qi] = T(0);
+        T run = T(0);
 #pragma unroll
-    for (int ch = 0; ch < NCH; ++ch) {
-        for (int rr = 0; rr < K; ++rr) {
-            const int r = K * ch + rr;
-            if (r >= F) break;
-            T v = __shfl_sync(0xffffffffu, q2[ch], rr << (5 - LOGK));
-            run += v;
-            if (lane == (r & 31)) incl[(K * ch) >> 5] = run;
+        for (int ch = 0; ch < NCH; ++ch) {
+            for (int rr = 0; rr < K; ++rr) {
+                const int r = K * ch + rr;
+                if (r >= F) break;
+                T v = __shfl_sync(0xffffffffu, q2[ch], rr << (5 - LOGK));
+                run += v;
+                if (lane == (r & 31)) incl[(K * ch) >> 5] = run;
+            }
         }
+        tot = run;
+    } else {
+        // FP32: lane l gathers the form of row l + 32 qi, then a warp
+        // inclusive scan per 32 rows with the carry of the previous ones
+        // (5 steps instead of F sequential ones; the FP32 mode is not tied
+        // to the reference's association)
+        constexpr int CPW = 32 / K;   // chunks per 32 rows
+        T carry = T(0);
+#pragma unroll
+        for (int qi = 0; qi < FQ; ++qi) {
+            T v = T(0);
+#pragma unroll
+            for (int cc = 0; cc < CPW; ++cc) {
+                if (qi * CPW + cc < NCH) {
+                    const T t = __shfl_sync(0xffffffffu, q2[qi * CPW + cc], (lane % K) << (5 - LOGK));
+                    if (lane / K == cc) v = t;
+                }
+            }
+            if (lane + 32 * qi >= F) v = T(0);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const T u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            incl[qi] = v + carry;
+            carry += __shfl_sync(0xffffffffu, v, 31);
+        }
+        tot = carry;
     }
-    const T tot = run;
     int res = F - 1;
     bool found = false;
 #pragma unroll
