@@ -38,6 +38,9 @@
 #ifndef FTL_DESC_WARPS32
 #define FTL_DESC_WARPS32 8         // warps per block for R <= 32
 #endif
+#ifndef FTL_DESC_WARPS128_F32
+#define FTL_DESC_WARPS128_F32 6    // FP32, R > 64: one block of 6 warps fills the shared memory
+#endif
 #ifndef FTL_DESC_REDO
 #define FTL_DESC_REDO 1            // FP32: flag samples that met a zero-mass block for the careful redo
 #endif
@@ -57,6 +60,16 @@ struct Shape {
     static constexpr int FQ = (RMAX + 31) / 32;   // leaf rows per lane (F <= R)
     static constexpr bool XX_SMEM = RMAX > 32 || FTL_DESC_XX_SMEM32;
     static constexpr int WARPS = RMAX <= 32 ? FTL_DESC_WARPS32 : (RMAX <= 64 ? 4 : 2);
+};
+
+// Warps per block of the draw kernels.  R > 64: each warp's slot holds the
+// 8256-entry packed outer product (33 KB in FP32, 66 KB in FP64) next to the
+// block's pair table (16.5 KB): 6 FP32 warps fit one block per SM (224 KB),
+// where blocks of 2 gave 2 blocks per SM (4 warps).
+template <int RMAX, typename T>
+struct Blk {
+    static constexpr int WARPS =
+        RMAX <= 64 ? Shape<RMAX>::WARPS : (sizeof(T) == 4 ? FTL_DESC_WARPS128_F32 : Shape<RMAX>::WARPS);
 };
 
 // 16-byte vector of the tree precision.

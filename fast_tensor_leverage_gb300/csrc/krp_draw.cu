@@ -177,13 +177,13 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
 }
 
 template <int RMAX, typename T, bool S32>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Blk<RMAX, T>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, T> dw;
     setup_draw_warp<RMAX, T>(dw, smem_raw, p.R, p.P, p.S);
     const int warp = threadIdx.x >> 5;
-    for (int64_t i = (int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp; i < p.J;
-         i += (int64_t)gridDim.x * Shape<RMAX>::WARPS)
+    for (int64_t i = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; i < p.J;
+         i += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS)
         draw_sample<RMAX, T, false, S32>(p, i, dw);
 }
 
@@ -198,14 +198,14 @@ struct MultiDrawParams {
 };
 
 template <int RMAX, typename T, bool S32>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Blk<RMAX, T>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, T> dw;
     setup_draw_warp<RMAX, T>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
     const int warp = threadIdx.x >> 5;
     const int64_t total = mp.cum[mp.n];
-    for (int64_t g = (int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp; g < total;
-         g += (int64_t)gridDim.x * Shape<RMAX>::WARPS) {
+    for (int64_t g = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; g < total;
+         g += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS) {
         int r = 0;
         while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
         draw_sample<RMAX, T, false, S32>(mp.req[r], g - mp.cum[r], dw);
@@ -227,13 +227,13 @@ __device__ __forceinline__ bool needs_redo(const DrawParams &p, int64_t i) {
 }
 
 template <int RMAX, bool S32>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_kernel(DrawParams p) {
+__global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_kernel(DrawParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, float> dw;
     setup_draw_warp<RMAX, float>(dw, smem_raw, p.R, p.P, p.S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t nw = (int64_t)gridDim.x * Shape<RMAX>::WARPS;
-    for (int64_t b = ((int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp) * 32; b < p.J; b += nw * 32) {
+    const int64_t nw = (int64_t)gridDim.x * Blk<RMAX, float>::WARPS;
+    for (int64_t b = ((int64_t)blockIdx.x * Blk<RMAX, float>::WARPS + warp) * 32; b < p.J; b += nw * 32) {
         unsigned bal = __ballot_sync(0xffffffffu, needs_redo<RMAX>(p, b + lane));
         while (bal) {
             const int src = __ffs(bal) - 1;
@@ -244,14 +244,14 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_kernel(Draw
 }
 
 template <int RMAX, bool S32>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32) krp_fixup_multi_kernel(MultiDrawParams mp) {
+__global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_multi_kernel(MultiDrawParams mp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     DrawWarp<RMAX, float> dw;
     setup_draw_warp<RMAX, float>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t total = mp.cum[mp.n];
-    const int64_t nw = (int64_t)gridDim.x * Shape<RMAX>::WARPS;
-    for (int64_t b = ((int64_t)blockIdx.x * Shape<RMAX>::WARPS + warp) * 32; b < total; b += nw * 32) {
+    const int64_t nw = (int64_t)gridDim.x * Blk<RMAX, float>::WARPS;
+    for (int64_t b = ((int64_t)blockIdx.x * Blk<RMAX, float>::WARPS + warp) * 32; b < total; b += nw * 32) {
         const int64_t g = b + lane;
         int r = 0;
         while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
@@ -281,7 +281,7 @@ struct TreeSampleParams {
 // PartitionTree::PTSample_internal (cpp_ext/partition_tree.hpp:232-405):
 // x = scaled_h[i]; samples[i] = selected row; h[i] o= U[row].
 template <int RMAX, typename T>
-__global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Shape<RMAX>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Blk<RMAX, T>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -298,8 +298,8 @@ __global__ void __launch_bounds__(Shape<RMAX>::WARPS * 32, (sizeof(T) == 4 ? FTL
     qf.P = P;
     qf.S = p.S;
     qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
-    for (int64_t i = (int64_t)blockIdx.x * S::WARPS + warp; i < p.J;
-         i += (int64_t)gridDim.x * S::WARPS) {
+    for (int64_t i = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; i < p.J;
+         i += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS) {
         double x[XPL];
 #pragma unroll
         for (int q = 0; q < XPL; ++q) {
@@ -350,12 +350,12 @@ __global__ void philox_fill_kernel(double *out, int64_t n, uint64_t seed, uint64
 template <int RMAX, typename T>
 static size_t desc_smem() {
     return (NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16 +
-           (size_t)Shape<RMAX>::WARPS * WarpSlot<RMAX, T>::bytes;
+           (size_t)Blk<RMAX, T>::WARPS * WarpSlot<RMAX, T>::bytes;
 }
 
 template <int RMAX, typename T, bool S32>
 static int launch_draw(const DrawParams &p, cudaStream_t st) {
-    const int warps = Shape<RMAX>::WARPS;
+    const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
     static bool attr = false;
     if (!attr) {
@@ -382,7 +382,7 @@ static int launch_draw(const DrawParams &p, cudaStream_t st) {
 
 template <int RMAX, typename T, bool S32>
 static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
-    const int warps = Shape<RMAX>::WARPS;
+    const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
     static bool attr = false;
     if (!attr) {
@@ -410,7 +410,7 @@ static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
 
 template <int RMAX, typename T>
 static int launch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
-    const int warps = Shape<RMAX>::WARPS;
+    const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
     static bool attr = false;
     if (!attr) {
