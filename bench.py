@@ -75,6 +75,29 @@ def dist_setup():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    """The largest value of x over the ranks (x itself on one rank): the
+    timed region of the slowest replica sets the whole-job time."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seeds(rank: int) -> dict:
+    """Seeds of one replica: every rank draws its own factors and uniforms,
+    so the replicas do independent work (weak scaling, no exchange)."""
+    return {"factors": 1234 + rank, "sampler": 7 + rank, "sparse": 2024 + rank, "serve": 2024 + rank}
+
+
+def whole_job_rate(ws: int, units_per_rank: float, seconds: float) -> float:
+    """Units all ranks processed per second of the slowest rank's time."""
+    return ws * units_per_rank / seconds
+
+
 # ------------------------------------------------------------------ clocks
 
 class ClockSampler:
@@ -227,7 +250,8 @@ def run_ours(args, ws, rank, local):
         dist.init_process_group("nccl", device_id=dev)
     N, I, R, J = args.N, 1 << args.log2I, args.R, args.J
     j = N + 1
-    U = make_factors_device(N, I, R, 1234 + rank, dev)
+    seeds = replica_seeds(rank)
+    U = make_factors_device(N, I, R, seeds["factors"], dev)
     st = torch.cuda.current_stream(dev)
 
     def barrier():
@@ -251,17 +275,13 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize(dev)
         barrier()
         clk = clocks.stop() if clocks else None
-        ms = e0.elapsed_time(e1) / steps
-        if ws > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, ws, dev)
         return ms, clk
 
-    s = ftl.Sampler(U, J, R, "efficient", precision=args.precision, seed=7 + rank)
+    s = ftl.Sampler(U, J, R, "efficient", precision=args.precision, seed=seeds["sampler"])
     clocks = ClockSampler(local) if rank == 0 else None
     ms, clk = time_draws(s, args.steps, args.warmup, clocks)
-    value = ws * J / (ms / 1e3)
+    value = whole_job_rate(ws, J, ms / 1e3)
 
     # descent kernel alone (roofline): computeM once, then timed launches
     _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), j, st.cuda_stream)
@@ -299,12 +319,8 @@ def run_ours(args, ws, rank, local):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         s.KRPDrawSamples_materialize(j, samples_np, h_np, w_np, draws=draws_host)
-    t_e2e = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = {"value": ws * J * e2e_steps / t_e2e, "unit": UNIT,
+    t_e2e = max_over_ranks(time.perf_counter() - t0, ws, dev)
+    e2e = {"value": whole_job_rate(ws, J * e2e_steps, t_e2e), "unit": UNIT,
            "h2d_bytes_per_step": 2 * N * J * 8,
            "d2h_bytes_per_step": N * J * 8 + J * R * 8 + J * 8,
            "api": "Sampler.KRPDrawSamples_materialize(j, samples, h_out, weights_out, draws=pinned host uniforms)"}
@@ -314,9 +330,9 @@ def run_ours(args, ws, rank, local):
     if args.precision == "fp32" and not args.no_fp64_arm:
         del s
         torch.cuda.empty_cache()
-        s64 = ftl.Sampler(U, J, R, "efficient", precision="fp64", seed=7 + rank)
+        s64 = ftl.Sampler(U, J, R, "efficient", precision="fp64", seed=seeds["sampler"])
         ms64, _ = time_draws(s64, max(10, args.steps // 5), max(3, args.warmup // 4))
-        fp64 = {"value": ws * J / (ms64 / 1e3), "ms_per_step": ms64}
+        fp64 = {"value": whole_job_rate(ws, J, ms64 / 1e3), "ms_per_step": ms64}
         del s64
 
     cpu = None
@@ -431,7 +447,7 @@ def run_als(args, ws, rank, local):
     dev = torch.device("cuda", local)
     dims = [4_800_000, 1_800_000, 1_800_000]
     R, J = 25, 1 << 16
-    idx, vals = sparse_powerlaw_tensor(dims, int(args.nnz), 1.1, seed=2024 + rank, device=dev)
+    idx, vals = sparse_powerlaw_tensor(dims, int(args.nnz), 1.1, seed=replica_seeds(rank)["sparse"], device=dev)
     t0 = time.perf_counter()
     sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
     torch.cuda.synchronize(dev)
@@ -556,7 +572,8 @@ def run_serve(args, ws, rank, local):
     del warm
     torch.cuda.synchronize(dev)
     torch.cuda.empty_cache()   # the warm-up engine's cached blocks belong to its streams
-    stream = S.poisson_request_stream(2024 + rank, args.rate, args.duration, als_fraction=args.als_fraction)
+    stream = S.poisson_request_stream(replica_seeds(rank)["serve"], args.rate, args.duration,
+                                      als_fraction=args.als_fraction)
     # the sparse tensors of CP-ALS requests are request payloads: made on the
     # device before the clock starts (sampling factors are made at admission)
     for _, r in stream:
