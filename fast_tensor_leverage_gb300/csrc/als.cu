@@ -328,16 +328,35 @@ __global__ void mttkrp_kernel(const uint64_t *__restrict__ skeys, const uint32_t
 // instead of R per touched nonzero.
 constexpr int MTT_CHUNK = 512;
 
+// uw[u] = w[urep[u]] for every unique sample (walked through the occupied
+// table slots, the only places slot_uidx is written), so the MTTKRP loads
+// the weight of a hit next to its representative instead of after it.
+__global__ void unique_weight_kernel(const uint64_t *__restrict__ tkeys, const int32_t *__restrict__ slot_uidx,
+                                     int64_t T, const int32_t *__restrict__ urep, const double *__restrict__ w,
+                                     double *__restrict__ uw) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < T; s += (int64_t)gridDim.x * blockDim.x) {
+        if (tkeys[s] != kEmpty) {
+            const int32_t u = slot_uidx[s];
+            uw[u] = w[urep[u]];
+        }
+    }
+}
+
+// Lanes probe 32 nonzeros at a time (key and unique index of a slot read in
+// the same round trip); the hits are then applied in nonzero order, G at a
+// time: their h rows (lane = column, CPL columns per lane) are loaded
+// together before the ordered accumulation, so the row loads of G hits
+// overlap instead of following one another.
+template <int CPL, int G>
 __global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
                                    const double *__restrict__ rvals, int64_t nnz,
                                    const uint64_t *__restrict__ tkeys, const int32_t *__restrict__ slot_uidx,
                                    int64_t T, const int32_t *__restrict__ urep, const int32_t *__restrict__ ucnt,
-                                   const double *__restrict__ w, const double *__restrict__ h, int R,
+                                   const double *__restrict__ uw, const double *__restrict__ h, int R,
                                    double *__restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    constexpr int CPL = (FTL_MAX_RANK + 31) / 32;
     const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
     for (int64_t ch = gw; ch < nchunks; ch += nw) {
         const int64_t z0 = ch * MTT_CHUNK, z1 = min(nnz, z0 + MTT_CHUNK);
@@ -355,8 +374,9 @@ __global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint
                 int32_t u = -1;
                 for (int64_t probe = 0; probe < T; ++probe) {
                     const uint64_t k = tkeys[s];
+                    const int32_t su = slot_uidx[s];
                     if (k == key) {
-                        u = slot_uidx[s];
+                        u = su;
                         break;
                     }
                     if (k == kEmpty) break;
@@ -365,32 +385,51 @@ __global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint
                 if (u >= 0) {
                     rep = urep[u];
                     row = rrows[z];
-                    coef = rvals[z] * w[rep] * (double)ucnt[u];
+                    coef = rvals[z] * uw[u] * (double)ucnt[u];
                 }
             }
             unsigned hits = __ballot_sync(0xffffffffu, rep >= 0);
             while (hits) {
-                const int src = __ffs(hits) - 1;
-                hits &= hits - 1;
-                const int32_t hrep = __shfl_sync(0xffffffffu, rep, src);
-                const int32_t hrow = __shfl_sync(0xffffffffu, row, src);
-                const double cf = __shfl_sync(0xffffffffu, coef, src);
-                if (hrow != cur) {
-                    if (cur >= 0) {
+                int32_t hrep[G], hrow[G];
+                double cf[G], hv[G][CPL];
+                int nh = 0;
 #pragma unroll
-                        for (int c = 0; c < CPL; ++c) {
-                            const int col = lane + 32 * c;
-                            if (col < R) atomicAdd(out + (int64_t)cur * R + col, acc[c]);
-                            acc[c] = 0.0;
-                        }
+                for (int g = 0; g < G; ++g) {
+                    int src = 0;
+                    if (hits) {
+                        src = __ffs(hits) - 1;
+                        hits &= hits - 1;
+                        nh = g + 1;
                     }
-                    cur = hrow;
+                    hrep[g] = __shfl_sync(0xffffffffu, rep, src);
+                    hrow[g] = __shfl_sync(0xffffffffu, row, src);
+                    cf[g] = __shfl_sync(0xffffffffu, coef, src);
                 }
-                const double *hr = h + (int64_t)hrep * R;
 #pragma unroll
-                for (int c = 0; c < CPL; ++c) {
-                    const int col = lane + 32 * c;
-                    if (col < R) acc[c] = fma(cf, hr[col], acc[c]);
+                for (int g = 0; g < G; ++g) {
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) {
+                        const int col = lane + 32 * c;
+                        hv[g][c] = (g < nh && col < R) ? h[(int64_t)hrep[g] * R + col] : 0.0;
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (g < nh) {
+                        if (hrow[g] != cur) {
+                            if (cur >= 0) {
+#pragma unroll
+                                for (int c = 0; c < CPL; ++c) {
+                                    const int col = lane + 32 * c;
+                                    if (col < R) atomicAdd(out + (int64_t)cur * R + col, acc[c]);
+                                    acc[c] = 0.0;
+                                }
+                            }
+                            cur = hrow[g];
+                        }
+#pragma unroll
+                        for (int c = 0; c < CPL; ++c) acc[c] = fma(cf[g], hv[g][c], acc[c]);
+                    }
                 }
             }
         }
@@ -717,7 +756,9 @@ extern "C" int ftl_sparse_gather(const int64_t *perm, const uint32_t *idx, const
 
 extern "C" int ftl_dedup_workspace_bytes(int64_t J, size_t *out) {
     FTL_CHECK_ARG(out && J >= 1 && J <= INT32_MAX / 2, "ftl_dedup_workspace_bytes: bad J=%lld", (long long)J);
-    *out = (size_t)table_size_for(J) * (sizeof(uint64_t) + 3 * sizeof(int32_t));
+    // slot keys, first, count, unique index; then one weight per unique sample
+    const size_t T = (size_t)table_size_for(J);
+    *out = T * (sizeof(uint64_t) + 3 * sizeof(int32_t)) + (size_t)J * sizeof(double);
     return FTL_OK;
 }
 
@@ -754,10 +795,21 @@ extern "C" int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *ro
     const int64_t T = table_size_for(J);
     const uint64_t *tk = (const uint64_t *)dedup_workspace;
     const int32_t *tu = (const int32_t *)(tk + T) + 2 * T;
+    // T is a power of two >= 1024, so the weights after the T int32 slots are 8-byte aligned
+    double *uw = (double *)((char *)dedup_workspace + (size_t)T * (sizeof(uint64_t) + 3 * sizeof(int32_t)));
+    unique_weight_kernel<<<grid_for(T), 256, 0, st>>>(tk, tu, T, urep, w, uw);
     const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
     int blocks = (int)std::min<int64_t>((nchunks * 32 + 255) / 256, (int64_t)num_sms() * 32);
-    mttkrp_rows_kernel<<<std::max(blocks, 1), 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep,
-                                                             ucnt, w, h, R, out);
+    blocks = std::max(blocks, 1);
+    if (R <= 32)
+        mttkrp_rows_kernel<1, 8><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep, ucnt, uw,
+                                                         h, R, out);
+    else if (R <= 64)
+        mttkrp_rows_kernel<2, 4><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep, ucnt, uw,
+                                                         h, R, out);
+    else
+        mttkrp_rows_kernel<4, 2><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep, ucnt, uw,
+                                                         h, R, out);
     return check_launch("mttkrp_rows_kernel");
 }
 
