@@ -76,7 +76,7 @@ class ALS:
         self._gram = torch.empty((R, R), dtype=torch.float64, device=dev)
         self._pinv = torch.empty((R, R), dtype=torch.float64, device=dev)
         self._vscr = torch.empty((R, R), dtype=torch.float64, device=dev)
-        self._mttkrp = torch.empty(max(lr.dims) * R, dtype=torch.float64, device=dev)
+        self._hp = torch.empty((J, R), dtype=torch.float64, device=dev)   # sampled rows times pinv
         self._dims_c = (ctypes.c_int64 * lr.N)(*lr.dims)
         # every buffer an update uses is sized here, so updates (and captured
         # sweeps) allocate nothing
@@ -112,24 +112,29 @@ class ALS:
         _lib.call("ftl_pinv_square", self._gram.data_ptr(), R, R, self._nuniq.data_ptr(), 1e-11,
                   self._pinv.data_ptr(), self._vscr.data_ptr(), st)
         I_j = lr.dims[j]
-        mt = self._mttkrp[: I_j * R]
+        # U_j = MTTKRP pinv (als.hpp:189-203) with MTTKRP = sum_z coef_z e_row(z)
+        # h_rep(z)^T, i.e. U_j = sum_z coef_z e_row(z) (h_rep(z)^T pinv): the J
+        # sampled rows are multiplied by pinv first (J x R^2 FP64 instead of
+        # I_j x R^2) and the MTTKRP accumulates straight into U_j.
+        hp = self._hp
+        _lib.call("ftl_solve_rows", h.data_ptr(), self._pinv.data_ptr(), J, R, hp.data_ptr(), st)
+        out = lr.U_dev[j]
         if not isinstance(gt, SparseTensor):
             # black-box right-hand side (black_box_tensor.hpp:21-67): low-rank
             # shortcut or dense fiber gather, rows past gt.dims[j] zeroed
             gt._sampled_mttkrp_dev(samples.data_ptr(), J, self._urep.data_ptr(), self._ucnt.data_ptr(),
-                                   self._nuniq.data_ptr(), w.data_ptr(), h.data_ptr(), R, j, mt.data_ptr(), I_j, st)
+                                   self._nuniq.data_ptr(), w.data_ptr(), hp.data_ptr(), R, j, out.data_ptr(), I_j, st)
         elif I_j == gt.dims[j]:
             # one balanced pass over the nonzeros sorted by output row
             rrows, rkeys, rvals = gt.rows[j]
             _lib.call("ftl_sparse_mttkrp_rows", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), gt.nnz,
                       self._ws.get("dedup", nb).data_ptr(), J, self._urep.data_ptr(), self._ucnt.data_ptr(),
-                      w.data_ptr(), h.data_ptr(), R, mt.data_ptr(), I_j, st)
+                      w.data_ptr(), hp.data_ptr(), R, out.data_ptr(), I_j, st)
         else:
             skeys, idxj, vj = gt.lookups[j]
             _lib.call("ftl_sparse_mttkrp", skeys.data_ptr(), idxj.data_ptr(), vj.data_ptr(), gt.nnz,
                       self._ukeys.data_ptr(), self._urep.data_ptr(), w.data_ptr(), self._ucnt.data_ptr(),
-                      self._nuniq.data_ptr(), J, h.data_ptr(), R, mt.data_ptr(), I_j, st)
-        _lib.call("ftl_solve_rows", mt.data_ptr(), self._pinv.data_ptr(), I_j, R, lr.U_dev[j].data_ptr(), st)
+                      self._nuniq.data_ptr(), J, hp.data_ptr(), R, out.data_ptr(), I_j, st)
         if renormalize:
             lr.renormalize_columns(j)          # mirrors to the host array when lr.sync_host
         elif lr.sync_host:
