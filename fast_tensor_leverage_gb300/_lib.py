@@ -104,7 +104,9 @@ SIGNATURES = {
     "ftl_weighted_gram": ([_P, _P, _P, _P, _P, _I64, _INT, _P, ctypes.c_size_t, _P, _P], _INT),
     "ftl_pinv_square": ([_P, _INT, _INT, _P, ctypes.c_double, _P, _P, _P], _INT),
     "ftl_sparse_mttkrp": ([_P, _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _INT, _P, _I64, _P], _INT),
-    "ftl_sparse_mttkrp_rows": ([_P, _P, _P, _I64, _P, _I64, _P, _P, _P, _P, _INT, _P, _I64, _P], _INT),
+    "ftl_mttkrp_rows_workspace_bytes": ([_I64, _INT, _SZP], _INT),
+    "ftl_sparse_mttkrp_rows": ([_P, _P, _P, _I64, _P, _P, _P, _P, _I64, _I64, _P, _P, _INT, _P, ctypes.c_size_t, _P, _I64, _P],
+                               _INT),
     "ftl_solve_rows": ([_P, _P, _I64, _INT, _P, _P], _INT),
     "ftl_colnorm_workspace_bytes": ([_INT, _SZP], _INT),
     "ftl_renormalize_columns": ([_P, _I64, _INT, _P, _P, ctypes.c_size_t, _INT, _P], _INT),
@@ -159,7 +161,7 @@ def tree_bytes(n: int, F: int, R: int, prec: int) -> int:
 
 
 def ws_bytes(name: str, *args) -> int:
-    """Workspace size query: name is one of dedup / gram / colnorm / fit."""
+    """Workspace size query: name is one of dedup / mttkrp_rows / gram / colnorm / fit / ..."""
     out = ctypes.c_size_t()
     call(f"ftl_{name}_workspace_bytes", *args, ctypes.byref(out))
     return out.value

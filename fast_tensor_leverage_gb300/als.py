@@ -81,6 +81,8 @@ class ALS:
         # every buffer an update uses is sized here, so updates (and captured
         # sweeps) allocate nothing
         self._ws.get("dedup", _lib.ws_bytes("dedup", J))
+        if isinstance(self.ground_truth, SparseTensor):
+            self._ws.get("mttkrp_rows", _lib.ws_bytes("mttkrp_rows", J, R))
         if isinstance(self.ground_truth, LowRankTensor):
             self.ground_truth._ws.get("lowrank_mttkrp", _lib.ws_bytes("lowrank_mttkrp", self.ground_truth.R, R))
         self._ws.get("gram", _lib.ws_bytes("gram", R))
@@ -127,9 +129,11 @@ class ALS:
         elif I_j == gt.dims[j]:
             # one balanced pass over the nonzeros sorted by output row
             rrows, rkeys, rvals = gt.rows[j]
+            mb = _lib.ws_bytes("mttkrp_rows", J, R)
             _lib.call("ftl_sparse_mttkrp_rows", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), gt.nnz,
-                      self._ws.get("dedup", nb).data_ptr(), J, self._urep.data_ptr(), self._ucnt.data_ptr(),
-                      w.data_ptr(), hp.data_ptr(), R, out.data_ptr(), I_j, st)
+                      self._ukeys.data_ptr(), self._urep.data_ptr(), self._ucnt.data_ptr(), self._nuniq.data_ptr(),
+                      J, J, w.data_ptr(), hp.data_ptr(), R, self._ws.get("mttkrp_rows", mb).data_ptr(), mb,
+                      out.data_ptr(), I_j, st)
         else:
             skeys, idxj, vj = gt.lookups[j]
             _lib.call("ftl_sparse_mttkrp", skeys.data_ptr(), idxj.data_ptr(), vj.data_ptr(), gt.nnz,

@@ -321,77 +321,136 @@ __global__ void mttkrp_kernel(const uint64_t *__restrict__ skeys, const uint32_t
 // Row-grouped MTTKRP (the same sum as mttkrp_kernel): nonzeros sorted by
 // their mode-j index, each carrying its row and fiber key.  The sorted
 // nonzeros are cut into fixed chunks of MTT_CHUNK, one warp per chunk, so
-// work is balanced however skewed the rows are.  Lanes probe the dedup hash
-// table for 32 nonzeros at a time; hits are applied in nonzero order to a
-// per-row accumulator (lane = column) that is flushed with one atomic add
-// per column whenever the row changes -- a handful of atomics per chunk
+// work is balanced however skewed the rows are.  Lanes probe a table of the
+// unique fibers for 32 nonzeros at a time; hits are applied in nonzero order
+// to a per-row accumulator (lane = column) that is flushed with one atomic
+// add per column whenever the row changes -- a handful of atomics per chunk
 // instead of R per touched nonzero.
 constexpr int MTT_CHUNK = 512;
+#ifndef FTL_MTT_MINB
+#define FTL_MTT_MINB 4
+#endif
+#ifndef FTL_MTT_G
+#define FTL_MTT_G 4
+#endif
 
-// uw[u] = w[urep[u]] for every unique sample (walked through the occupied
-// table slots, the only places slot_uidx is written), so the MTTKRP loads
-// the weight of a hit next to its representative instead of after it.
-__global__ void unique_weight_kernel(const uint64_t *__restrict__ tkeys, const int32_t *__restrict__ slot_uidx,
-                                     int64_t T, const int32_t *__restrict__ urep, const double *__restrict__ w,
-                                     double *__restrict__ uw) {
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < T; s += (int64_t)gridDim.x * blockDim.x) {
-        if (tkeys[s] != kEmpty) {
-            const int32_t u = slot_uidx[s];
-            uw[u] = w[urep[u]];
+// Probe table of the unique fibers: 16-byte slots {fiber key, unique index},
+// open addressing with linear probing, at most 1/4 full (slots = power of two
+// >= 4 J), Fibonacci hashing (key * 2^64/phi, top bits).
+constexpr uint64_t kFib = 0x9E3779B97F4A7C15ull;
+
+static int64_t probe_slots_for(int64_t J) {
+    int64_t T = 1024;
+    while (T < 4 * J) T <<= 1;
+    return T;
+}
+
+static int log2_exact(int64_t T) {
+    int l = 0;
+    while ((int64_t(1) << l) < T) ++l;
+    return l;
+}
+
+static int padded_rank(int R) { return (R + 3) & ~3; }
+
+__global__ void probe_insert_kernel(const uint64_t *__restrict__ ukeys, const int64_t *__restrict__ nq_dev,
+                                    int64_t nq_host, ulonglong2 *__restrict__ pt, int64_t T, int shift) {
+    const int64_t nq = nq_dev ? *nq_dev : nq_host;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nq; u += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = ukeys[u];
+        uint64_t s = (key * kFib) >> shift;
+        // the keys are distinct, so a slot is either free or holds another key
+        for (int64_t probe = 0; probe < T; ++probe) {
+            const unsigned long long prev =
+                atomicCAS((unsigned long long *)&pt[s].x, (unsigned long long)kEmpty, (unsigned long long)key);
+            if (prev == kEmpty) {
+                pt[s].y = (unsigned long long)u;
+                break;
+            }
+            s = (s + 1) & (uint64_t)(T - 1);
         }
     }
 }
 
-// Lanes probe 32 nonzeros at a time (key and unique index of a slot read in
-// the same round trip); the hits are then applied in nonzero order, G at a
-// time: their h rows (lane = column, CPL columns per lane) are loaded
-// together before the ordered accumulation, so the row loads of G hits
-// overlap instead of following one another.
+// hs[u, c] = s_u lhs[rep(u), c] with s_u = (w ? w[rep(u)] : 1) (cnt ? cnt[u] : 1),
+// row stride Rp (columns R..Rp-1 zero).
+__global__ void scaled_unique_rows_kernel(const int32_t *__restrict__ urep, const int32_t *__restrict__ ucnt,
+                                          const double *__restrict__ w, const int64_t *__restrict__ nq_dev,
+                                          int64_t nq_host, const double *__restrict__ lhs, int R, int Rp,
+                                          double *__restrict__ hs) {
+    const int64_t nq = nq_dev ? *nq_dev : nq_host;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nq * Rp;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = e / Rp;
+        const int c = (int)(e - u * Rp);
+        double v = 0.0;
+        if (c < R) {
+            const int64_t rep = urep[u];
+            const double sc = (w ? w[rep] : 1.0) * (ucnt ? (double)ucnt[u] : 1.0);
+            v = sc * lhs[rep * R + c];
+        }
+        hs[e] = v;
+    }
+}
+
+// One warp per chunk.  The key, row and value of the next 32 nonzeros are
+// loaded before the current 32 are probed, so the streaming loads overlap
+// the probes and the hit processing (a deeper pipeline that also issued the
+// next batch's first probe early measured no faster).  Hits are applied G at a time: their
+// scaled rows (lane = column, CPL columns per lane) are loaded together before
+// the ordered accumulation.
 template <int CPL, int G>
-__global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
-                                   const double *__restrict__ rvals, int64_t nnz,
-                                   const uint64_t *__restrict__ tkeys, const int32_t *__restrict__ slot_uidx,
-                                   int64_t T, const int32_t *__restrict__ urep, const int32_t *__restrict__ ucnt,
-                                   const double *__restrict__ uw, const double *__restrict__ h, int R,
-                                   double *__restrict__ out) {
+__global__ void __launch_bounds__(256, FTL_MTT_MINB)
+    mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
+                       const double *__restrict__ rvals, int64_t nnz, const ulonglong2 *__restrict__ pt, int64_t T,
+                       int shift, const double *__restrict__ hs, int R, int Rp, double *__restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
+    const uint64_t mask = (uint64_t)(T - 1);
     for (int64_t ch = gw; ch < nchunks; ch += nw) {
         const int64_t z0 = ch * MTT_CHUNK, z1 = min(nnz, z0 + MTT_CHUNK);
         double acc[CPL];
 #pragma unroll
         for (int c = 0; c < CPL; ++c) acc[c] = 0.0;
         int32_t cur = -1;  // row held in acc (warp-uniform)
+        uint64_t nkey = kEmpty;
+        int32_t nrow = 0;
+        double nval = 0.0;
+        if (z0 + lane < z1) {
+            nkey = rkeys[z0 + lane];
+            nrow = rrows[z0 + lane];
+            nval = rvals[z0 + lane];
+        }
         for (int64_t zb = z0; zb < z1; zb += 32) {
-            const int64_t z = zb + lane;
-            int32_t rep = -1, row = -1;
-            double coef = 0.0;
-            if (z < z1) {
-                const uint64_t key = rkeys[z];
-                uint64_t s = mix64(key) & (uint64_t)(T - 1);
-                int32_t u = -1;
+            const uint64_t key = nkey;
+            const int32_t row = nrow;
+            const double val = nval;
+            const int64_t zn = zb + 32 + lane;
+            nkey = kEmpty;
+            if (zn < z1) {
+                nkey = rkeys[zn];
+                nrow = rrows[zn];
+                nval = rvals[zn];
+            }
+            int32_t u = -1;
+            if (key != kEmpty) {
+                uint64_t s = (key * kFib) >> shift;
                 for (int64_t probe = 0; probe < T; ++probe) {
-                    const uint64_t k = tkeys[s];
-                    const int32_t su = slot_uidx[s];
-                    if (k == key) {
-                        u = su;
+                    const ulonglong2 e = pt[s];
+                    if (e.x == key) {
+                        u = (int32_t)e.y;
                         break;
                     }
-                    if (k == kEmpty) break;
-                    s = (s + 1) & (uint64_t)(T - 1);
-                }
-                if (u >= 0) {
-                    rep = urep[u];
-                    row = rrows[z];
-                    coef = rvals[z] * uw[u] * (double)ucnt[u];
+                    if (e.x == kEmpty) break;
+                    s = (s + 1) & mask;
                 }
             }
-            unsigned hits = __ballot_sync(0xffffffffu, rep >= 0);
+            unsigned hits = __ballot_sync(0xffffffffu, u >= 0);
             while (hits) {
-                int32_t hrep[G], hrow[G];
-                double cf[G], hv[G][CPL];
+                int32_t hu[G], hrow[G];
+                double hval[G], hv[G][CPL];
                 int nh = 0;
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
@@ -401,16 +460,16 @@ __global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint
                         hits &= hits - 1;
                         nh = g + 1;
                     }
-                    hrep[g] = __shfl_sync(0xffffffffu, rep, src);
+                    hu[g] = __shfl_sync(0xffffffffu, u, src);
                     hrow[g] = __shfl_sync(0xffffffffu, row, src);
-                    cf[g] = __shfl_sync(0xffffffffu, coef, src);
+                    hval[g] = __shfl_sync(0xffffffffu, val, src);
                 }
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
 #pragma unroll
                     for (int c = 0; c < CPL; ++c) {
                         const int col = lane + 32 * c;
-                        hv[g][c] = (g < nh && col < R) ? h[(int64_t)hrep[g] * R + col] : 0.0;
+                        hv[g][c] = (g < nh && col < Rp) ? hs[(int64_t)hu[g] * Rp + col] : 0.0;
                     }
                 }
 #pragma unroll
@@ -428,7 +487,7 @@ __global__ void mttkrp_rows_kernel(const int32_t *__restrict__ rrows, const uint
                             cur = hrow[g];
                         }
 #pragma unroll
-                        for (int c = 0; c < CPL; ++c) acc[c] = fma(cf[g], hv[g][c], acc[c]);
+                        for (int c = 0; c < CPL; ++c) acc[c] = fma(hval[g], hv[g][c], acc[c]);
                     }
                 }
             }
@@ -756,9 +815,9 @@ extern "C" int ftl_sparse_gather(const int64_t *perm, const uint32_t *idx, const
 
 extern "C" int ftl_dedup_workspace_bytes(int64_t J, size_t *out) {
     FTL_CHECK_ARG(out && J >= 1 && J <= INT32_MAX / 2, "ftl_dedup_workspace_bytes: bad J=%lld", (long long)J);
-    // slot keys, first, count, unique index; then one weight per unique sample
+    // slot keys, first, count, unique index
     const size_t T = (size_t)table_size_for(J);
-    *out = T * (sizeof(uint64_t) + 3 * sizeof(int32_t)) + (size_t)J * sizeof(double);
+    *out = T * (sizeof(uint64_t) + 3 * sizeof(int32_t));
     return FTL_OK;
 }
 
@@ -781,35 +840,54 @@ extern "C" int ftl_dedup(const uint64_t *keys, int64_t J, void *workspace, size_
     return check_launch("dedup kernels");
 }
 
+extern "C" int ftl_mttkrp_rows_workspace_bytes(int64_t J, int R, size_t *out) {
+    FTL_CHECK_ARG(out && J >= 1 && J <= INT32_MAX / 4 && R >= 1 && R <= FTL_MAX_RANK,
+                  "ftl_mttkrp_rows_workspace_bytes: bad J=%lld or R=%d", (long long)J, R);
+    // probe table, then the scaled unique rows (16-byte aligned: slots are 16 B)
+    *out = (size_t)probe_slots_for(J) * sizeof(ulonglong2) + (size_t)J * padded_rank(R) * sizeof(double);
+    return FTL_OK;
+}
+
 extern "C" int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *row_keys, const double *row_vals,
-                                      int64_t nnz, const void *dedup_workspace, int64_t J, const int32_t *urep,
-                                      const int32_t *ucnt, const double *w, const double *h, int R, double *out,
+                                      int64_t nnz, const uint64_t *ukeys, const int32_t *urep, const int32_t *ucnt,
+                                      const int64_t *num_unique_dev, int64_t num_unique, int64_t J, const double *w,
+                                      const double *h, int R, void *workspace, size_t ws_bytes, double *out,
                                       int64_t I_j, void *stream) {
-    FTL_CHECK_ARG(row_idx && row_keys && row_vals && dedup_workspace && urep && ucnt && w && h && out,
+    FTL_CHECK_ARG(row_idx && row_keys && row_vals && ukeys && urep && h && workspace && out,
                   "ftl_sparse_mttkrp_rows: null pointer");
-    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1 && J >= 1 && nnz >= 0, "ftl_sparse_mttkrp_rows: bad shape");
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && I_j >= 1 && J >= 1 && nnz >= 0 && num_unique >= 0 &&
+                      num_unique <= J,
+                  "ftl_sparse_mttkrp_rows: bad shape");
+    size_t need = 0;
+    int rc = ftl_mttkrp_rows_workspace_bytes(J, R, &need);
+    if (rc) return rc;
+    FTL_CHECK_ARG(ws_bytes >= need, "ftl_sparse_mttkrp_rows: workspace %zu < %zu bytes", ws_bytes, need);
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t err = cudaMemsetAsync(out, 0, (size_t)I_j * R * sizeof(double), st);
     if (err != cudaSuccess) return fail(FTL_E_CUDA, "ftl_sparse_mttkrp_rows: memset: %s", cudaGetErrorString(err));
     if (nnz == 0) return FTL_OK;
-    const int64_t T = table_size_for(J);
-    const uint64_t *tk = (const uint64_t *)dedup_workspace;
-    const int32_t *tu = (const int32_t *)(tk + T) + 2 * T;
-    // T is a power of two >= 1024, so the weights after the T int32 slots are 8-byte aligned
-    double *uw = (double *)((char *)dedup_workspace + (size_t)T * (sizeof(uint64_t) + 3 * sizeof(int32_t)));
-    unique_weight_kernel<<<grid_for(T), 256, 0, st>>>(tk, tu, T, urep, w, uw);
+    const int64_t T = probe_slots_for(J);
+    const int shift = 64 - log2_exact(T);
+    const int Rp = padded_rank(R);
+    ulonglong2 *pt = (ulonglong2 *)workspace;
+    double *hs = (double *)(pt + T);
+    err = cudaMemsetAsync(pt, 0xFF, (size_t)T * sizeof(ulonglong2), st);
+    if (err != cudaSuccess) return fail(FTL_E_CUDA, "ftl_sparse_mttkrp_rows: memset: %s", cudaGetErrorString(err));
+    probe_insert_kernel<<<grid_for(J), 256, 0, st>>>(ukeys, num_unique_dev, num_unique, pt, T, shift);
+    scaled_unique_rows_kernel<<<grid_for(J * Rp), 256, 0, st>>>(urep, ucnt, w, num_unique_dev, num_unique, h, R, Rp,
+                                                                 hs);
     const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
     int blocks = (int)std::min<int64_t>((nchunks * 32 + 255) / 256, (int64_t)num_sms() * 32);
     blocks = std::max(blocks, 1);
     if (R <= 32)
-        mttkrp_rows_kernel<1, 8><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep, ucnt, uw,
-                                                         h, R, out);
+        mttkrp_rows_kernel<1, FTL_MTT_G><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, pt, T, shift, hs,
+                                                                 R, Rp, out);
     else if (R <= 64)
-        mttkrp_rows_kernel<2, 4><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep, ucnt, uw,
-                                                         h, R, out);
+        mttkrp_rows_kernel<2, 4><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, pt, T, shift, hs, R, Rp,
+                                                         out);
     else
-        mttkrp_rows_kernel<4, 2><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, tk, tu, T, urep, ucnt, uw,
-                                                         h, R, out);
+        mttkrp_rows_kernel<4, 2><<<blocks, 256, 0, st>>>(row_idx, row_keys, row_vals, nnz, pt, T, shift, hs, R, Rp,
+                                                         out);
     return check_launch("mttkrp_rows_kernel");
 }
 

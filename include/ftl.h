@@ -231,14 +231,21 @@ int ftl_sparse_mttkrp(const uint64_t *sorted_keys, const uint32_t *sorted_idxj,
 
 /* The same MTTKRP grouped by output row: nonzeros sorted by their mode-j
  * index, given as row_idx (that index), row_keys (fiber keys) and row_vals;
- * queries are the unique fibers of the last ftl_dedup on dedup_workspace
- * (sized for J).  One pass over the nonzeros in fixed chunks (balanced under
- * any row skew), per-row accumulation, one atomic add per row segment; out
- * (I_j x R) is zeroed first. */
+ * the queries are the unique fibers ukeys[u] with rows urep[u] and
+ * multiplicities ucnt[u], u < (num_unique_dev ? *num_unique_dev :
+ * num_unique), as ftl_dedup returns them; each query's nonzeros add
+ * value * s_u * lhs[urep[u]] to out[idx_j], s_u = (w ? w[urep[u]] : 1) *
+ * (ucnt ? ucnt[u] : 1).  One pass over the nonzeros in fixed chunks
+ * (balanced under any row skew), probing a device table of the queries,
+ * per-row accumulation, one atomic add per row segment; out (I_j x R) is
+ * zeroed first.  Workspace: ftl_mttkrp_rows_workspace_bytes(J, R). */
+int ftl_mttkrp_rows_workspace_bytes(int64_t J, int R, size_t *out);
 int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *row_keys,
-                           const double *row_vals, int64_t nnz, const void *dedup_workspace,
-                           int64_t J, const int32_t *urep, const int32_t *ucnt, const double *w,
-                           const double *h, int R, double *out, int64_t I_j, void *stream);
+                           const double *row_vals, int64_t nnz, const uint64_t *ukeys,
+                           const int32_t *urep, const int32_t *ucnt,
+                           const int64_t *num_unique_dev, int64_t num_unique, int64_t J,
+                           const double *w, const double *h, int R, void *workspace,
+                           size_t ws_bytes, double *out, int64_t I_j, void *stream);
 
 /* U = B pinv row by row (pinv R x R symmetric); all-zero rows of B give zero
  * rows without arithmetic.  Replaces the cblas_dsymm of
