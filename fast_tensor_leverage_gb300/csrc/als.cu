@@ -254,6 +254,14 @@ __global__ void gram_reduce_kernel(const double *__restrict__ partial, int nblk,
 // triangle), keep eigenpair v (ascending rank r) when r >= R - target and
 // lambda > tol, out = sum_kept v v^T / lambda.  target = min(cap, R) with cap
 // read from *rank_cap when given.
+//
+// When every eigenpair is kept (target = R) and M is safely positive
+// definite, that sum is M^-1, computed here from the Cholesky factor M = L L^T
+// as L^-T L^-1 (R sequential steps instead of Jacobi sweeps).  The fast path
+// is taken when the factorisation succeeds and ||M^-1||_F < 1 / (2 tol): then
+// lambda_min(M) = 1 / ||M^-1||_2 >= 1 / ||M^-1||_F > 2 tol, so the reference
+// keeps every eigenpair too.  Otherwise M is reloaded and the Jacobi path
+// runs.
 __global__ void pinv_square_kernel(const double *__restrict__ M, int R, int target, const int64_t *rank_cap,
                                    double tol, double *__restrict__ out, double *vscratch) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -264,6 +272,46 @@ __global__ void pinv_square_kernel(const double *__restrict__ M, int R, int targ
     int *pq = (int *)(cs + R + 2);
     int *order = pq + R + 2;
     int *flag = order + R;
+    int tr = target;
+    if (rank_cap) tr = (int)min((int64_t)R, *rank_cap);
+    if (tr >= R) {
+        for (int e = tid; e < RR; e += nth) {
+            int a = e / R, b = e - a * R;
+            A[e] = a <= b ? M[e] : M[b * R + a];
+        }
+        __syncthreads();
+        if (cholesky_lower(A, R, 0.0, flag)) {
+            // X = L^-1 (lower), column c by forward substitution, into V
+            for (int c = tid; c < R; c += nth) {
+                for (int i = 0; i < c; ++i) V[i * R + c] = 0.0;
+                for (int i = c; i < R; ++i) {
+                    double t = (i == c) ? 1.0 : 0.0;
+                    for (int k = c; k < i; ++k) t -= A[i * R + k] * V[k * R + c];
+                    V[i * R + c] = t / A[i * R + i];
+                }
+            }
+            __syncthreads();
+            // out = X^T X; cs[0] accumulates ||out||_F^2
+            if (tid == 0) cs[0] = 0.0;
+            __syncthreads();
+            double fro = 0.0;
+            for (int e = tid; e < RR; e += nth) {
+                int a = e / R, b = e - a * R;
+                const int k0 = a > b ? a : b;
+                double t = 0.0;
+                for (int k = k0; k < R; ++k) t += V[k * R + a] * V[k * R + b];
+                out[e] = t;
+                fro += t * t;
+            }
+            for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+            if ((tid & 31) == 0) atomicAdd(cs, fro);
+            __syncthreads();
+            const bool ok = cs[0] == cs[0] && 4.0 * tol * tol * cs[0] < 1.0;
+            __syncthreads();
+            if (ok) return;
+        }
+        __syncthreads();
+    }
     for (int e = tid; e < RR; e += nth) {
         int a = e / R, b = e - a * R;
         A[e] = a <= b ? M[e] : M[b * R + a];
@@ -271,8 +319,6 @@ __global__ void pinv_square_kernel(const double *__restrict__ M, int R, int targ
     __syncthreads();
     jacobi_eigen<double>(A, V, R, cs, pq, flag);
     sort_ascending<double>(A, R, order);
-    int tr = target;
-    if (rank_cap) tr = (int)min((int64_t)R, *rank_cap);
     for (int e = tid; e < RR; e += nth) {
         int a = e / R, b = e - a * R;
         double s = 0.0;

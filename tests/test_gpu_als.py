@@ -329,3 +329,59 @@ def test_gpu_blackbox_downsampled_mttkrp_and_exact_update(ftl, name):
     Uj = mt @ O.pinv_square(G, Rl, 1e-11)
     n = np.linalg.norm(Uj, axis=0)
     np.testing.assert_allclose(U[j], Uj / n, rtol=0, atol=1e-9 * np.abs(Uj / n).max())
+
+
+def _pinv_gpu(M, R, target, cap=None):
+    from fast_tensor_leverage_gb300 import _lib
+    Md = torch.as_tensor(M, device="cuda")
+    out = torch.empty_like(Md)
+    vs = torch.empty_like(Md)
+    capd = None if cap is None else torch.tensor([cap], dtype=torch.int64, device="cuda")
+    _lib.call("ftl_pinv_square", Md.data_ptr(), R, target, None if capd is None else capd.data_ptr(), 1e-11,
+              out.data_ptr(), vs.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    return out.cpu().numpy()
+
+
+def _spd(rng, R, lam):
+    Q, _ = np.linalg.qr(rng.normal(size=(R, R)))
+    return (Q * lam) @ Q.T
+
+
+@pytest.mark.parametrize("R", [1, 5, 25, 64, 128])
+def test_pinv_square_well_conditioned(ftl, R):
+    """Positive definite Grams (the Cholesky path): the pseudo-inverse equals
+    the oracle's eigen-based one to 1e-11 relative (Frobenius)."""
+    rng = np.random.default_rng(90 + R)
+    B = rng.normal(size=(3 * R, R))
+    M = B.T @ B * 1e3
+    ref = O.pinv_square(M, R, 1e-11)
+    got = _pinv_gpu(M, R, R)
+    assert np.linalg.norm(got - ref) <= 1e-11 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("R", [6, 25, 100])
+def test_pinv_square_drops_eigenvalues_like_the_reference(ftl, R):
+    """Eigenvalues at or below the 1e-11 cut, exact zeros (rank-deficient
+    Grams) and a rank cap below R take the eigen path: the same eigenpairs are
+    kept as in the oracle."""
+    rng = np.random.default_rng(190 + R)
+    lam = np.exp(rng.uniform(-2, 2, size=R))
+    # an eigenvalue below the cut: dropped
+    lam1 = lam.copy()
+    lam1[0] = 4e-12
+    M = _spd(rng, R, lam1)
+    ref = O.pinv_square(M, R, 1e-11)
+    got = _pinv_gpu(M, R, R)
+    assert np.linalg.norm(got - ref) <= 1e-8 * np.linalg.norm(ref)
+    # rank-deficient Gram (three exact zero directions)
+    B = rng.normal(size=(R, R - 3))
+    M = B @ B.T
+    ref = O.pinv_square(M, R, 1e-11)
+    got = _pinv_gpu(M, R, R)
+    assert np.linalg.norm(got - ref) <= 1e-8 * np.linalg.norm(ref)
+    # rank cap below R (fewer unique samples than R): the R - cap smallest dropped
+    M = _spd(rng, R, lam)
+    for cap in (R - 2, 1):
+        ref = O.pinv_square(M, cap, 1e-11)
+        assert np.linalg.norm(_pinv_gpu(M, R, R, cap=cap) - ref) <= 1e-9 * np.linalg.norm(ref)
+        assert np.linalg.norm(_pinv_gpu(M, R, cap) - ref) <= 1e-9 * np.linalg.norm(ref)
