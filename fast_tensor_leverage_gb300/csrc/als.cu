@@ -125,20 +125,48 @@ __global__ void table_insert_kernel(const uint64_t *__restrict__ skeys, int64_t 
     }
 }
 
-// Deterministic compaction in slot order (one CTA of 1024 threads).
-__global__ void table_compact_kernel(const uint64_t *keys, const int32_t *first, const int32_t *count, int64_t T,
-                                     uint64_t *ukeys, int32_t *urep, int32_t *ucnt, int64_t *num_unique,
-                                     int32_t *slot_uidx) {
+// Deterministic compaction in slot order, in two launches: the table is cut
+// into slices of `slice` slots, one CTA each; table_count_kernel counts each
+// slice's occupied slots, table_write_kernel offsets its slice by the counts
+// of the slices before it and writes the unique keys in slot order.
+__global__ void table_count_kernel(const uint64_t *__restrict__ keys, int64_t T, int64_t slice,
+                                   int32_t *__restrict__ bcount) {
+    __shared__ int warp_tot[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t b0 = blockIdx.x * slice, b1 = min(T, b0 + slice);
+    int c = 0;
+    for (int64_t s = b0 + tid; s < b1; s += blockDim.x) c += keys[s] != kEmpty ? 1 : 0;
+    c = __reduce_add_sync(0xffffffffu, (unsigned)c);
+    if (lane == 0) warp_tot[warp] = c;
+    __syncthreads();
+    if (tid == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_tot[w];
+        bcount[blockIdx.x] = t;
+    }
+}
+
+__global__ void table_write_kernel(const uint64_t *__restrict__ keys, const int32_t *__restrict__ first,
+                                   const int32_t *__restrict__ count, int64_t T, int64_t slice,
+                                   const int32_t *__restrict__ bcount, uint64_t *__restrict__ ukeys,
+                                   int32_t *__restrict__ urep, int32_t *__restrict__ ucnt,
+                                   int64_t *__restrict__ num_unique) {
     __shared__ int warp_tot[32];
     __shared__ int64_t base_s;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) base_s = 0;
+    if (warp == 0) {
+        int64_t t = 0;
+        for (int b = lane; b < (int)blockIdx.x; b += 32) t += bcount[b];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) base_s = t;
+    }
     __syncthreads();
-    for (int64_t off = 0; off < T; off += blockDim.x) {
+    const int64_t b0 = blockIdx.x * slice, b1 = min(T, b0 + slice);
+    for (int64_t off = b0; off < b1; off += blockDim.x) {
         const int64_t s = off + tid;
-        const int occ = (s < T && keys[s] != kEmpty) ? 1 : 0;
-        unsigned bal = __ballot_sync(0xffffffffu, occ);
-        int pre = __popc(bal & ((1u << lane) - 1));
+        const int occ = (s < b1 && keys[s] != kEmpty) ? 1 : 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, occ);
+        const int pre = __popc(bal & ((1u << lane) - 1));
         if (lane == 0) warp_tot[warp] = __popc(bal);
         __syncthreads();
         int wbase = 0, total = 0;
@@ -147,17 +175,24 @@ __global__ void table_compact_kernel(const uint64_t *keys, const int32_t *first,
             total += warp_tot[w];
         }
         if (occ) {
-            int64_t o = base_s + wbase + pre;
+            const int64_t o = base_s + wbase + pre;
             ukeys[o] = keys[s];
             urep[o] = first[s];
             ucnt[o] = count[s];
-            slot_uidx[s] = (int32_t)o;
         }
         __syncthreads();
         if (tid == 0) base_s += total;
         __syncthreads();
     }
-    if (tid == 0) *num_unique = base_s;
+    if (tid == 0 && blockIdx.x == gridDim.x - 1) *num_unique = base_s;
+}
+
+// Slice of the compaction: 2048 slots, doubled until there are at most 1024
+// slices (T is a power of two >= 1024).
+static int64_t compact_slice(int64_t T) {
+    int64_t sl = 2048;
+    while (T / sl > 1024) sl <<= 1;
+    return sl;
 }
 
 static int64_t table_size_for(int64_t J) {
@@ -170,81 +205,97 @@ static int64_t table_size_for(int64_t J) {
 
 // partial[b][e] = sum over this block's rows u of s_u * h_a h_b, e = packed
 // (a, b); rows u < *n_rows (or n_rows_host), h row = lhs[row(u)], s_u =
-// (w ? w[row(u)] : 1) * (cnt ? cnt[u] : 1).  All-zero rows are skipped (they
-// add exact zeros): most rows of a sampled-ALS factor are zero, and this is
-// FP64 arithmetic at a low issue rate.
+// (w ? w[row(u)] : 1) * (cnt ? cnt[u] : 1).  Rows are staged 32 at a time
+// with their scaled copy s_u h; each thread owns up to GRAM_EPT packed
+// entries (thread t: entries t, t + blockDim, ...; up to 9 covers R = 128,
+// 8256 entries, on 1024 threads) and adds one FMA per
+// entry and row.  All-zero rows are skipped (they add exact zeros): most
+// rows of a sampled-ALS factor are zero, and this is FP64 arithmetic at a
+// low issue rate.
+static int gram_threads(int R) {
+    const int P = packed_size(R);
+    return std::min(1024, (P + 31) / 32 * 32);
+}
+
+template <int GRAM_EPT>
 __global__ void gram_partial_kernel(const double *__restrict__ lhs, const int32_t *__restrict__ rowidx,
                                     const double *__restrict__ w, const int32_t *__restrict__ cnt,
                                     const int64_t *__restrict__ n_rows_dev, int64_t n_rows_host, int R,
                                     double *__restrict__ partial) {
-    extern __shared__ double hs[];  // 32 rows x R, then 32 scale slots
+    extern __shared__ double hs[];  // 32 rows x R, 32 scaled rows x R
     __shared__ int nz[32];          // row has a nonzero entry
     const int P = packed_size(R);
     const int64_t n = n_rows_dev ? *n_rows_dev : n_rows_host;
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
-    double *sc = hs + 32 * R;
-    // entries are covered in passes of 4 per thread
-    for (int e0 = 0; e0 < P; e0 += 4 * blockDim.x) {
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        int ea[4], eb[4];
+    double *hsc = hs + 32 * R;
+    double acc[GRAM_EPT];
+    int ea[GRAM_EPT], eb[GRAM_EPT];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            int e = e0 + threadIdx.x + t * blockDim.x;
-            ea[t] = eb[t] = -1;
-            if (e < P) {
-                int a = 0, rem = e;
-                while (rem >= R - a) {
-                    rem -= R - a;
-                    ++a;
-                }
-                ea[t] = a;
-                eb[t] = a + rem;
+    for (int t = 0; t < GRAM_EPT; ++t) {
+        acc[t] = 0.0;
+        const int e = threadIdx.x + t * blockDim.x;
+        ea[t] = eb[t] = -1;
+        if (e < P) {
+            int a = 0, rem = e;
+            while (rem >= R - a) {
+                rem -= R - a;
+                ++a;
             }
+            ea[t] = a;
+            eb[t] = a + rem;
         }
-        for (int64_t u0 = r0; u0 < r1; u0 += 32) {
-            const int m = (int)min((int64_t)32, r1 - u0);
-            __syncthreads();
-            if (threadIdx.x < 32) nz[threadIdx.x] = 0;
-            __syncthreads();
-            for (int e = threadIdx.x; e < m * R; e += blockDim.x) {
-                int uu = e / R, col = e - uu * R;
-                int64_t u = u0 + uu;
-                int64_t row = rowidx ? rowidx[u] : u;
-                const double v = lhs[row * R + col];
-                hs[e] = v;
-                if (v != 0.0) nz[uu] = 1;
-            }
-            for (int uu = threadIdx.x; uu < m; uu += blockDim.x) {
-                int64_t u = u0 + uu;
-                int64_t row = rowidx ? rowidx[u] : u;
-                sc[uu] = (w ? w[row] : 1.0) * (cnt ? (double)cnt[u] : 1.0);
-            }
-            __syncthreads();
-            for (int uu = 0; uu < m; ++uu) {
-                if (!nz[uu]) continue;
-                const double *hr = hs + uu * R;
-                const double su = sc[uu];
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    if (ea[t] >= 0) acc[t] = fma(su * hr[ea[t]], hr[eb[t]], acc[t]);
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-            if (ea[t] >= 0) partial[(int64_t)blockIdx.x * P + e0 + threadIdx.x + t * blockDim.x] = acc[t];
     }
+    for (int64_t u0 = r0; u0 < r1; u0 += 32) {
+        const int m = (int)min((int64_t)32, r1 - u0);
+        __syncthreads();
+        if (threadIdx.x < 32) nz[threadIdx.x] = 0;
+        __syncthreads();
+        for (int e = threadIdx.x; e < m * R; e += blockDim.x) {
+            const int uu = e / R;
+            const int64_t u = u0 + uu;
+            const int64_t row = rowidx ? rowidx[u] : u;
+            const double v = lhs[row * R + (e - uu * R)];
+            const double su = (w ? w[row] : 1.0) * (cnt ? (double)cnt[u] : 1.0);
+            hs[e] = v;
+            hsc[e] = su * v;
+            if (v != 0.0) nz[uu] = 1;
+        }
+        __syncthreads();
+        for (int uu = 0; uu < m; ++uu) {
+            if (!nz[uu]) continue;
+            const double *hr = hs + uu * R;
+            const double *hq = hsc + uu * R;
+#pragma unroll
+            for (int t = 0; t < GRAM_EPT; ++t)
+                if (ea[t] >= 0) acc[t] = fma(hq[ea[t]], hr[eb[t]], acc[t]);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < GRAM_EPT; ++t)
+        if (ea[t] >= 0) partial[(int64_t)blockIdx.x * P + threadIdx.x + t * blockDim.x] = acc[t];
 }
 
-// out (R x R, full symmetric) = sum of the partials in block order.
+// out (R x R, full symmetric) = sum of the partials; one warp per packed
+// entry, lanes over the blocks.
 __global__ void gram_reduce_kernel(const double *__restrict__ partial, int nblk, int R, double *__restrict__ out) {
     const int P = packed_size(R);
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < R * R; e += gridDim.x * blockDim.x) {
-        int a = e / R, b = e - a * R;
-        int pe = packed_index(min(a, b), max(a, b), R);
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int pe = wg; pe < P; pe += nw) {
         double s = 0.0;
-        for (int k = 0; k < nblk; ++k) s += partial[(int64_t)k * P + pe];
-        out[e] = s;
+        for (int k = lane; k < nblk; k += 32) s += partial[(int64_t)k * P + pe];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            int a = 0, rem = pe;
+            while (rem >= R - a) {
+                rem -= R - a;
+                ++a;
+            }
+            const int b = a + rem;
+            out[a * R + b] = s;
+            out[b * R + a] = s;
+        }
     }
 }
 
@@ -280,7 +331,7 @@ __global__ void pinv_square_kernel(const double *__restrict__ M, int R, int targ
             A[e] = a <= b ? M[e] : M[b * R + a];
         }
         __syncthreads();
-        if (cholesky_lower(A, R, 0.0, flag)) {
+        if (cholesky_lower(A, R, 0.0, flag, cs + 1)) {
             // X = L^-1 (lower), column c by forward substitution, into V
             for (int c = tid; c < R; c += nth) {
                 for (int i = 0; i < c; ++i) V[i * R + c] = 0.0;
@@ -669,14 +720,17 @@ __global__ void solve_rows_kernel(const double *__restrict__ B, const double *__
     }
 }
 
+// Thread t owns column t % R of rows t / R, t / R + rows_per_pass, ... (a
+// block covers rows_per_pass whole rows per step, so loads are contiguous).
 __global__ void colsq_partial_kernel(const double *__restrict__ U, int64_t I, int R, double *__restrict__ partial) {
-    // thread t accumulates column (t % R) over rows t / R, t / R + stride ...
     const int tid = threadIdx.x;
     const int rows_per_pass = blockDim.x / R;
     double acc = 0.0;
     const int col = tid % R, r_in = tid / R;
     if (r_in < rows_per_pass) {
-        for (int64_t r = (int64_t)blockIdx.x * rows_per_pass + r_in; r < I; r += (int64_t)gridDim.x * rows_per_pass) {
+        const int64_t step = (int64_t)gridDim.x * rows_per_pass;
+#pragma unroll 4
+        for (int64_t r = (int64_t)blockIdx.x * rows_per_pass + r_in; r < I; r += step) {
             double x = U[r * R + col];
             acc = fma(x, x, acc);
         }
@@ -691,13 +745,18 @@ __global__ void colsq_partial_kernel(const double *__restrict__ U, int64_t I, in
     }
 }
 
-// norms: sqrt of the column sums, <= 1e-7 -> 1 (low_rank_tensor.hpp:229-238)
+// norms: sqrt of the column sums, <= 1e-7 -> 1 (low_rank_tensor.hpp:229-238);
+// one warp per column, lanes over the block partials.
 __global__ void colnorm_finish_kernel(const double *__restrict__ partial, int nblk, int R, double *__restrict__ norms) {
-    for (int c = threadIdx.x; c < R; c += blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int c = threadIdx.x >> 5; c < R; c += nw) {
         double s = 0.0;
-        for (int k = 0; k < nblk; ++k) s += partial[(int64_t)k * R + c];
-        double n = sqrt(s);
-        norms[c] = n <= 1e-7 ? 1.0 : n;
+        for (int k = lane; k < nblk; k += 32) s += partial[(int64_t)k * R + c];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            const double n = sqrt(s);
+            norms[c] = n <= 1e-7 ? 1.0 : n;
+        }
     }
 }
 
@@ -708,9 +767,14 @@ __global__ void colscale_kernel(double *__restrict__ U, int64_t I, int R, const 
     __shared__ double inv[FTL_MAX_RANK];
     for (int c = threadIdx.x; c < R; c += blockDim.x) inv[c] = 1.0 / norms[c];
     __syncthreads();
-    const int64_t total = I * R;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
-        U[e] = U[e] * inv[e % R];
+    // same row ownership as colsq_partial_kernel: no per-element index division
+    const int rows_per_pass = blockDim.x / R;
+    const int col = threadIdx.x % R, r_in = threadIdx.x / R;
+    if (r_in >= rows_per_pass) return;
+    const double f = inv[col];
+    const int64_t step = (int64_t)gridDim.x * rows_per_pass;
+#pragma unroll 4
+    for (int64_t r = (int64_t)blockIdx.x * rows_per_pass + r_in; r < I; r += step) U[r * R + col] *= f;
 }
 
 // ------------------------------------------------------------ fit terms
@@ -861,9 +925,9 @@ extern "C" int ftl_sparse_gather(const int64_t *perm, const uint32_t *idx, const
 
 extern "C" int ftl_dedup_workspace_bytes(int64_t J, size_t *out) {
     FTL_CHECK_ARG(out && J >= 1 && J <= INT32_MAX / 2, "ftl_dedup_workspace_bytes: bad J=%lld", (long long)J);
-    // slot keys, first, count, unique index
+    // slot keys, first, count; then one count per compaction slice
     const size_t T = (size_t)table_size_for(J);
-    *out = T * (sizeof(uint64_t) + 3 * sizeof(int32_t));
+    *out = T * (sizeof(uint64_t) + 2 * sizeof(int32_t)) + (size_t)(T / compact_slice(T) + 1) * sizeof(int32_t);
     return FTL_OK;
 }
 
@@ -878,11 +942,14 @@ extern "C" int ftl_dedup(const uint64_t *keys, int64_t J, void *workspace, size_
     uint64_t *tk = (uint64_t *)workspace;
     int32_t *tf = (int32_t *)(tk + T);
     int32_t *tc = tf + T;
-    int32_t *tu = tc + T;
+    int32_t *bc = tc + T;
+    const int64_t slice = compact_slice(T);
+    const int nsl = (int)((T + slice - 1) / slice);
     cudaStream_t st = (cudaStream_t)stream;
     table_clear_kernel<<<grid_for(T), 256, 0, st>>>(tk, tf, tc, T);
     table_insert_kernel<<<grid_for(J), 256, 0, st>>>(keys, J, tk, tf, tc, T);
-    table_compact_kernel<<<1, 1024, 0, st>>>(tk, tf, tc, T, ukeys, urep, ucnt, num_unique, tu);
+    table_count_kernel<<<nsl, 256, 0, st>>>(tk, T, slice, bc);
+    table_write_kernel<<<nsl, 256, 0, st>>>(tk, tf, tc, T, slice, bc, ukeys, urep, ucnt, num_unique);
     return check_launch("dedup kernels");
 }
 
@@ -953,9 +1020,29 @@ extern "C" int ftl_weighted_gram(const double *lhs, const int32_t *rowidx, const
     FTL_CHECK_ARG(ws_bytes >= need, "ftl_weighted_gram: workspace %zu < %zu bytes", ws_bytes, need);
     const int nblk = num_sms();
     cudaStream_t st = (cudaStream_t)stream;
-    const size_t smem = (size_t)(32 * R + 32) * sizeof(double);
-    gram_partial_kernel<<<nblk, 256, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, (double *)workspace);
-    gram_reduce_kernel<<<std::max(1, (R * R + 255) / 256), 256, 0, st>>>((const double *)workspace, nblk, R, gram_out);
+    const size_t smem = (size_t)(64 * R) * sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(gram_partial_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        cudaFuncSetAttribute(gram_partial_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        cudaFuncSetAttribute(gram_partial_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        cudaFuncSetAttribute(gram_partial_kernel<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+        attr = true;
+    }
+    const int P = packed_size(R);
+    const int threads = gram_threads(R);
+    const int ept = (P + threads - 1) / threads;
+    double *part = (double *)workspace;
+    if (ept <= 1)
+        gram_partial_kernel<1><<<nblk, threads, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, part);
+    else if (ept <= 2)
+        gram_partial_kernel<2><<<nblk, threads, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, part);
+    else if (ept <= 4)
+        gram_partial_kernel<4><<<nblk, threads, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, part);
+    else
+        gram_partial_kernel<9><<<nblk, threads, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, part);
+    gram_reduce_kernel<<<std::max(1, (P * 32 + 255) / 256), 256, 0, st>>>((const double *)workspace, nblk, R,
+                                                                          gram_out);
     return check_launch("weighted gram kernels");
 }
 
@@ -1029,8 +1116,8 @@ extern "C" int ftl_renormalize_columns(double *U, int64_t I, int R, double *norm
     const int threads = std::max(R, 1024 / R * R);
     cudaStream_t st = (cudaStream_t)stream;
     colsq_partial_kernel<<<nblk, threads, 0, st>>>(U, I, R, (double *)workspace);
-    colnorm_finish_kernel<<<1, 128, 0, st>>>((const double *)workspace, nblk, R, norms_out);
-    if (apply) colscale_kernel<<<grid_for(I * R), 256, 0, st>>>(U, I, R, norms_out);
+    colnorm_finish_kernel<<<1, 1024, 0, st>>>((const double *)workspace, nblk, R, norms_out);
+    if (apply) colscale_kernel<<<nblk * 2, threads, 0, st>>>(U, I, R, norms_out);
     return check_launch("renormalize kernels");
 }
 

@@ -79,17 +79,13 @@ __global__ void computem_pinv_kernel(CMParams p) {
     bool chol = false;
     if (p.prec == FTL_PREC_FP32) {
         // Mixed mode: when every eigenvalue of M[0] exceeds the reference's
-        // 1e-8 cut (M[0] - 1e-8 I positive definite), its pseudo-inverse is
-        // the inverse, computed in FP64 from the Cholesky factor:
-        // pinv = L^-T L^-1.  Otherwise the Jacobi path below runs.
+        // 1e-8 cut, its pseudo-inverse is the inverse, computed in FP64 from
+        // the Cholesky factor: pinv = L^-T L^-1.  The cut is certified by
+        // ||pinv||_F < 1 / (2e-8): lambda_min = 1 / ||M^-1||_2 >= 1 /
+        // ||M^-1||_F > 2e-8.  Otherwise the Jacobi path below runs.
         for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
         __syncthreads();
-        chol = cholesky_lower(A, R, 1e-8, flag);
-        if (chol) {
-            for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
-            __syncthreads();
-            chol = cholesky_lower(A, R, 0.0, flag);
-        }
+        chol = cholesky_lower(A, R, 0.0, flag, cs + 1);
         if (chol) {
             // V = L^-1 (lower), one column per thread, forward substitution
             for (int jc = tid; jc < R; jc += nth) {
@@ -104,13 +100,21 @@ __global__ void computem_pinv_kernel(CMParams p) {
                 }
             }
             __syncthreads();
+            if (tid == 0) cs[0] = 0.0;
+            __syncthreads();
+            double fro = 0.0;
             for (int e = tid; e < RR; e += nth) {
                 int a = e / R, b = e - a * R;
                 int lo = max(a, b);
                 double acc = 0.0;
                 for (int kk = lo; kk < R; ++kk) acc += V[kk * R + a] * V[kk * R + b];
                 A[e] = acc;  // A is free again: the factor is no longer needed after this pass
+                fro += acc * acc;
             }
+            for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+            if ((tid & 31) == 0) atomicAdd(cs, fro);
+            __syncthreads();
+            chol = cs[0] == cs[0] && 4e-16 * cs[0] < 1.0;
             __syncthreads();
         }
     }
@@ -259,6 +263,10 @@ __global__ void computem_eig_kernel(CMParams p) {
     }
 }
 
+#ifndef FTL_CM_THREADS
+#define FTL_CM_THREADS 512
+#endif
+
 int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st) {
     CMParams p;
     p.N = plan->N;
@@ -282,13 +290,13 @@ int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st) 
         cudaFuncSetAttribute(computem_eig_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr_set = true;
     }
-    computem_pinv_kernel<<<1, 512, smem, st>>>(p);
+    computem_pinv_kernel<<<1, FTL_CM_THREADS, smem, st>>>(p);
     int rc = check_launch("computem_pinv_kernel");
     if (rc) return rc;
     if (plan->prec == FTL_PREC_FP64)
-        computem_eig_kernel<double><<<plan->N, 512, smem, st>>>(p);
+        computem_eig_kernel<double><<<plan->N, FTL_CM_THREADS, smem, st>>>(p);
     else
-        computem_eig_kernel<float><<<plan->N, 512, smem, st>>>(p);
+        computem_eig_kernel<float><<<plan->N, FTL_CM_THREADS, smem, st>>>(p);
     return check_launch("computem_eig_kernel");
 }
 

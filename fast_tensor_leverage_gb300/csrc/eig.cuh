@@ -131,8 +131,12 @@ __device__ void sort_ascending(const T *A, int R, int *order) {
 
 // In-place lower Cholesky factor of (A - shift I), A dense R x R FP64 in
 // shared memory (lower triangle used).  Returns true (block-uniformly) when
-// every pivot is positive, i.e. A - shift I is positive definite.
-__device__ inline bool cholesky_lower(double *A, int R, double shift, int *flag) {
+// every pivot is positive, i.e. A - shift I is positive definite.  The column
+// below a pivot is scaled by the pivot's reciprocal (one FP64 division per
+// step instead of one per entry); rinv is one shared-memory double of scratch
+// (no static shared memory here: the callers' kernels opt in to the whole
+// 227 KB as dynamic shared memory).
+__device__ inline bool cholesky_lower(double *A, int R, double shift, int *flag, double *rinv) {
     const int tid = threadIdx.x, nth = blockDim.x;
     if (tid == 0) *flag = 1;
     for (int e = tid; e < R; e += nth) A[e * R + e] -= shift;
@@ -141,12 +145,14 @@ __device__ inline bool cholesky_lower(double *A, int R, double shift, int *flag)
         if (tid == 0) {
             double d = A[k * R + k];
             if (!(d > 0.0)) *flag = 0;
-            A[k * R + k] = d > 0.0 ? sqrt(d) : 1.0;
+            const double l = d > 0.0 ? sqrt(d) : 1.0;
+            A[k * R + k] = l;
+            *rinv = 1.0 / l;
         }
         __syncthreads();
         if (*flag == 0) break;
-        const double lkk = A[k * R + k];
-        for (int i = k + 1 + tid; i < R; i += nth) A[i * R + k] /= lkk;
+        const double r = *rinv;
+        for (int i = k + 1 + tid; i < R; i += nth) A[i * R + k] *= r;
         __syncthreads();
         const int m = R - k - 1;
         for (int w = tid; w < m * m; w += nth) {

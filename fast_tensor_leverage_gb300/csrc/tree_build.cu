@@ -14,6 +14,7 @@
 // leaf Grams; the internal levels are a second, purely elementwise pass.
 #include <algorithm>
 #include <cstdio>
+#include <type_traits>
 
 #include "ftl_common.cuh"
 
@@ -47,17 +48,19 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
 
     for (int64_t batch = blockIdx.x; batch < nbatch; batch += gridDim.x) {
         const int64_t leaf0 = batch * LB;
-        // Stage LB blocks (rows past n and columns past R are zero).
-        const int64_t total = (int64_t)LB * blk_elems;
-        for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-            int64_t lb = e / blk_elems;
-            int64_t rem = e - lb * blk_elems;
-            int64_t r = rem / RP;
-            int col = (int)(rem - r * RP);
-            int64_t row = (leaf0 + lb) * F + r;
-            T v = T(0);
-            if (leaf0 + lb < leaf_count && row < n && col < R) v = (T)U[row * R + col];
-            Us[e] = v;
+        // Stage LB blocks (rows past n and columns past R are zero).  The LB
+        // blocks are LB * F consecutive rows of U, copied one row per warp.
+        const int64_t row0 = leaf0 * F;
+        const int nrows = LB * (int)F;
+        const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+#pragma unroll 4
+        for (int rr = threadIdx.x >> 5; rr < nrows; rr += nwarps) {
+            const int64_t row = row0 + rr;
+            for (int col = lane; col < RP; col += 32) {
+                T v = T(0);
+                if (row < n && col < R) v = (T)U[row * R + col];
+                Us[rr * RP + col] = v;
+            }
         }
         __syncthreads();
         const int work = LB * tiles;
@@ -110,17 +113,64 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
     }
 }
 
+__device__ __forceinline__ float4 vadd(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ double2 vadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
 // G[c] = G[2c+1] + G[2c+2] for c in [start, end) (S = node stride; the
-// zero padding sums to zero).
-template <typename T>
-__global__ void level_sum_kernel(T *__restrict__ G, int64_t start, int64_t end, int S) {
-    const int64_t total = (end - start) * (int64_t)S;
+// zero padding sums to zero), in 16-byte vectors (a node stride is a whole
+// number of them); V = the vector type, S16 = vectors per node, I = the
+// index type (32-bit when the level fits).
+template <typename V, typename I>
+__global__ void level_sum_kernel(V *__restrict__ G, int64_t start, int64_t end, int S16) {
+    const I total = (I)((end - start) * S16);
+    for (I e = (I)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (I)gridDim.x * blockDim.x) {
+        const I cc = e / (I)S16;
+        const int k = (int)(e - cc * (I)S16);
+        const int64_t c = start + (int64_t)cc;
+        const V a = G[(2 * c + 1) * S16 + k], b = G[(2 * c + 2) * S16 + k];
+        G[c * S16 + k] = vadd(a, b);
+    }
+}
+
+// H complete levels in one pass: for each node a of the top level (heap
+// indices [top_start, top_start + top_count)) and vector component k, the
+// 2^H descendants of a at depth H (already built) are loaded, then summed
+// pairwise bottom-up, writing every node of a's subtree above them (the same
+// parent = left + right association as level_sum_kernel).
+template <typename V, int H>
+__global__ void __launch_bounds__(256) levels_fused_kernel(V *__restrict__ G, int64_t top_start, int64_t top_count,
+                                                           int S16) {
+    const int64_t total = top_count * S16;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = start + e / S;
-        int k = (int)(e % S);
-        G[c * S + k] = G[(2 * c + 1) * S + k] + G[(2 * c + 2) * S + k];
+        const int64_t a = top_start + e / S16;
+        const int k = (int)(e % S16);
+        V x[1 << H];
+        const int64_t base = ((a + 1) << H) - 1;  // first descendant at depth H
+#pragma unroll
+        for (int i = 0; i < (1 << H); ++i) x[i] = G[(base + i) * S16 + k];
+#pragma unroll
+        for (int m = 1; m <= H; ++m) {
+            // nodes at height m above depth H: 2^(H-m) of them
+            const int64_t first = ((a + 1) << (H - m)) - 1;
+#pragma unroll
+            for (int i = 0; i < (1 << (H - m)); ++i) {
+                x[i] = vadd(x[2 * i], x[2 * i + 1]);
+                G[(first + i) * S16 + k] = x[i];
+            }
+        }
     }
+}
+
+static int sm_count();
+
+template <typename V, int H>
+static void launch_fused(V *G, int64_t top_start, int64_t top_count, int S16, cudaStream_t st) {
+    const int64_t total = top_count * S16;
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+    levels_fused_kernel<V, H><<<std::max(blocks, 1), 256, 0, st>>>(G, top_start, top_count, S16);
 }
 
 template <typename T>
@@ -174,20 +224,38 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     leaf_gram_kernel<T><<<grid, 256, smem, st>>>(U, n, R, RP, g, LB, G);
     int rc = check_launch("leaf_gram_kernel");
     if (rc) return rc;
-    int64_t start = geom.nodes_before_lfill;
-    int64_t end = geom.node_count - geom.leaf_count;
-    while (true) {
-        if (end > start) {
-            const int S = node_stride(R, sizeof(T));
-            int64_t total = (end - start) * (int64_t)S;
-            int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
-            level_sum_kernel<T><<<blocks, 256, 0, st>>>(G, start, end, S);
-            rc = check_launch("level_sum_kernel");
-            if (rc) return rc;
-        }
-        if (start <= 0) break;
-        end = start;
-        start = (start + 1) / 2 - 1;
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    const int S16 = node_stride(R, sizeof(T)) * (int)sizeof(T) / 16;
+    // internal nodes of the partial level (children: leaves of the last level)
+    const int64_t start = geom.nodes_before_lfill;
+    const int64_t end = geom.node_count - geom.leaf_count;
+    if (end > start) {
+        const int64_t total = (end - start) * (int64_t)S16;
+        const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+        if (total < (int64_t)INT32_MAX)
+            level_sum_kernel<V, uint32_t><<<blocks, 256, 0, st>>>((V *)G, start, end, S16);
+        else
+            level_sum_kernel<V, int64_t><<<blocks, 256, 0, st>>>((V *)G, start, end, S16);
+        rc = check_launch("level_sum_kernel");
+        if (rc) return rc;
+    }
+    // the complete levels lfill_level - 1 .. 0 (level d = heap [2^d - 1,
+    // 2^(d+1) - 1)), four at a time from the bottom
+    for (int64_t d = geom.lfill_level - 1; d >= 0;) {
+        const int h = (int)std::min<int64_t>(4, d + 1);
+        const int64_t top = d - h + 1;
+        const int64_t top_start = (int64_t(1) << top) - 1, top_count = int64_t(1) << top;
+        if (h == 4)
+            launch_fused<V, 4>((V *)G, top_start, top_count, S16, st);
+        else if (h == 3)
+            launch_fused<V, 3>((V *)G, top_start, top_count, S16, st);
+        else if (h == 2)
+            launch_fused<V, 2>((V *)G, top_start, top_count, S16, st);
+        else
+            launch_fused<V, 1>((V *)G, top_start, top_count, S16, st);
+        rc = check_launch("levels_fused_kernel");
+        if (rc) return rc;
+        d = top - 1;
     }
     return FTL_OK;
 }
