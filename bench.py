@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0)
     ap.add_argument("--max-active", type=int, default=32)
     ap.add_argument("--nnz", type=float, default=1.5e8)
+    ap.add_argument("--als-scale", type=float, default=1.0,
+                    help="als: dims and nnz times this factor (a smaller case of the same kernels, for profiling)")
     ap.add_argument("--sweeps", type=int, default=20)
     ap.add_argument("--no-fp64-arm", action="store_true")
     return ap.parse_args()
@@ -436,8 +438,13 @@ def run_reference(args, ws, rank):
 def run_als(args, ws, rank, local):
     """Randomized CP-ALS on the synthetic stand-in for amazon-reviews:
     dims 4.8e6 x 1.8e6 x 1.8e6, Zipf(1.1) indices, nnz unique tuples,
-    log(1 + lognormal) values; R = 25, J = 2^16; PyLowRank(seed) factors
-    renormalised once, then `sweeps` sweeps of one sampled update per mode.
+    log(1 + lognormal) values; R = 25, J = 2^16; factors initialised by the
+    reference's randomized range finder (SparseTensor.execute_rrf, seeded,
+    renormalised), then `sweeps` sweeps of one sampled update per mode.
+    (From Gaussian factors the first update of this tensor hits ~3 nonzeros:
+    J = 2^16 fibers drawn near-uniformly from 3.2e12, 1.5e8 of them occupied;
+    whether a trajectory recovers from a factor with one nonzero row or
+    collapses to a zero factor then turns on single samples.)
     Reports update-only seconds per sweep (device time) and the exact fit
     after the last sweep, for mixed-precision and FP64 sampling."""
     import torch
@@ -445,9 +452,10 @@ def run_als(args, ws, rank, local):
     from fast_tensor_leverage_gb300.synthetic import sparse_powerlaw_tensor
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    dims = [4_800_000, 1_800_000, 1_800_000]
+    dims = [int(d * args.als_scale) for d in (4_800_000, 1_800_000, 1_800_000)]
     R, J = 25, 1 << 16
-    idx, vals = sparse_powerlaw_tensor(dims, int(args.nnz), 1.1, seed=replica_seeds(rank)["sparse"], device=dev)
+    idx, vals = sparse_powerlaw_tensor(dims, int(args.nnz * args.als_scale), 1.1, seed=replica_seeds(rank)["sparse"],
+                                       device=dev)
     t0 = time.perf_counter()
     sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
     torch.cuda.synchronize(dev)
@@ -461,7 +469,7 @@ def run_als(args, ws, rank, local):
     # yardstick for the mixed-vs-FP64 fit gap
     for prec, sseed in (("fp32", 11), ("fp64", 11), ("fp64_seed12", 12)):
         lhs = ftl.PyLowRank(dims, R, seed=7, sync_host=False)
-        lhs.ten.renormalize_columns(-1)
+        sp.execute_rrf(lhs.ten, seed=7)
         als = ftl.ALS(lhs.ten, sp)
         als.initialize_ds_als(J, "efficient", precision=prec[:4], seed=sseed)
         fit0 = lhs.compute_exact_fit(rhs)
@@ -486,10 +494,11 @@ def run_als(args, ws, rank, local):
     if rank != 0:
         return None
     return {
-        "metric": "CP-ALS s/sweep (update only), synthetic sparse 4.8e6 x 1.8e6 x 1.8e6, R=25, J=2^16",
+        "metric": "CP-ALS s/sweep (update only), synthetic sparse {} x {} x {}, R=25, J=2^16".format(*dims),
         "value": out["fp32"]["s_per_sweep"], "unit": "s/sweep", "higher_is_better": False, "n_gpus": ws,
         "sweeps": args.sweeps, "dtype": "fp32 trees / fp64 solve", "data": "synthetic (seeded Zipf 1.1, log1p lognormal)",
-        "config": {"workload": "randomized CP-ALS (STS-CP)", "dims": dims, "nnz": sp.nnz, "R": R, "J": J},
+        "config": {"workload": "randomized CP-ALS (STS-CP)", "dims": dims, "nnz": sp.nnz, "R": R, "J": J,
+                   "init": "execute_rrf (randomized range finder), seed 7"},
         "tensor_build_s": t_build, "mixed": out["fp32"], "fp64": out["fp64"], "fp64_seed12": out["fp64_seed12"],
         "fit_gap_mixed_vs_fp64": out["fp32"]["fit_final"] - out["fp64"]["fit_final"],
         "fit_gap_fp64_seed_to_seed": out["fp64_seed12"]["fit_final"] - out["fp64"]["fit_final"],
