@@ -814,6 +814,44 @@ __global__ void residual_partial_kernel(const uint32_t *__restrict__ idx, const 
     }
 }
 
+// The same sum with one thread per nonzero (N a template constant, so the N
+// row pointers stay in registers): R x N FP64 products per nonzero as lane
+// operations.  The warp-per-nonzero form above spends most of its FP64 issue
+// on the warp reduction of each nonzero, and the FP64 pipe (one warp
+// instruction per 16 cycles per SM) is what bounds this pass.
+template <int N>
+__global__ void residual_thread_kernel(const uint32_t *__restrict__ idx, const double *__restrict__ vals,
+                                       int64_t nnz, FactorPtrs fp, const double *__restrict__ sigma, int R,
+                                       double *__restrict__ partial) {
+    __shared__ double sig[FTL_MAX_RANK];
+    __shared__ double red[32];
+    for (int r = threadIdx.x; r < R; r += blockDim.x) sig[r] = sigma[r];
+    __syncthreads();
+    double acc = 0.0;
+    for (int64_t z = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; z < nnz; z += (int64_t)gridDim.x * blockDim.x) {
+        const double *row[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) row[k] = fp.U[k] + (int64_t)idx[z * N + k] * R;
+        double m = 0.0;
+        for (int r = 0; r < R; ++r) {
+            double p = sig[r];
+#pragma unroll
+            for (int k = 0; k < N; ++k) p *= row[k][r];
+            m += p;
+        }
+        const double v = vals[z];
+        acc += v * v - 2.0 * m * v;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        partial[blockIdx.x] = t;
+    }
+}
+
 __global__ void sum_kernel(const double *__restrict__ partial, int n, double *__restrict__ out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double s = 0.0;
@@ -1139,7 +1177,15 @@ extern "C" int ftl_sparse_residual_terms(const uint32_t *idx, const double *vals
     for (int k = 0; k < FTL_MAX_MODES; ++k) fp.U[k] = k < N ? U_dev[k] : nullptr;
     const int nblk = num_sms() * 16;
     cudaStream_t st = (cudaStream_t)stream;
-    residual_partial_kernel<<<nblk, 256, 0, st>>>(idx, vals, nnz, N, fp, sigma, R, (double *)workspace);
+    double *part = (double *)workspace;
+    switch (N) {
+        case 2: residual_thread_kernel<2><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;
+        case 3: residual_thread_kernel<3><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;
+        case 4: residual_thread_kernel<4><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;
+        case 5: residual_thread_kernel<5><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;
+        case 6: residual_thread_kernel<6><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;
+        default: residual_partial_kernel<<<nblk, 256, 0, st>>>(idx, vals, nnz, N, fp, sigma, R, part);
+    }
     sum_kernel<<<1, 32, 0, st>>>((const double *)workspace, nblk, out);
     return check_launch("residual kernels");
 }
