@@ -86,6 +86,13 @@ class Sampler:
             self._cm_stream = torch.cuda.Stream(dev, priority=-1)
             self._cm_done = [torch.cuda.Event() for _ in self._ws_sets]
             self._set_free = [None] * len(self._ws_sets)
+        # (set, j) of a computeM launched ahead for the next draw: after two
+        # draws with the same j, the next draw's computeM (same trees, same
+        # j: the same result) is launched right behind the current descent,
+        # so callers that wait for every draw (copies to the host) still get
+        # it overlapped.  Each draw still runs exactly one computeM.
+        self._spec = None
+        self._last_j = None
         self._tree_ev = torch.cuda.Event()
         self._refresh_plan()
         for k in range(N):
@@ -121,6 +128,12 @@ class Sampler:
     def update_sampler(self, j: int, stream=None) -> None:
         """Rebuild the Gram tree of factor j from its device copy
         (EfficientKRPSampler::update_sampler, efficient_krp_sampler.hpp:73-75)."""
+        if getattr(self, "_spec", None) is not None:
+            # a computeM launched ahead reads the trees: let it finish, then
+            # drop it (its result belongs to the old trees)
+            main = stream if stream is not None else torch.cuda.current_stream(self.device)
+            main.wait_event(self._cm_done[self._spec[0]])
+            self._spec = None
         _lib.call("ftl_tree_build", self.U[j].data_ptr(), self.dims[j], self.R, self.F[j],
                   self._prec, self.trees[j].data_ptr(), self._stream(stream))
         if self.U32 is not None:
@@ -157,14 +170,9 @@ class Sampler:
             b = self._next_set
             self._next_set = (b + 1) % len(self._plans)
             plan, cm = self._plans[b], self._cm_stream
-            # computeM(b) after the trees it reads and after the descent that
-            # last read workspace set b (it does not need the uniforms, so it
-            # is launched before they are copied); the descent after it
-            cm.wait_event(self._tree_ev)
-            if self._set_free[b] is not None:
-                cm.wait_event(self._set_free[b])
-            _lib.call("ftl_krp_compute_m", ctypes.byref(plan), j, int(cm.cuda_stream))
-            self._cm_done[b].record(cm)
+            if self._spec != (b, j):
+                self._launch_computem(b, j)
+            self._spec = None
         d_ptr = None
         if draws is not None:
             n = 2 * self.N * self.J
@@ -189,6 +197,11 @@ class Sampler:
             self._set_free[b] = ev
             self._plan = plan
             self.eig_G, self.M, self.lam, self.pinv32 = self._ws_sets[b]
+            if self._last_j == j:
+                nb = self._next_set
+                self._launch_computem(nb, j)
+                self._spec = (nb, j)
+            self._last_j = j
         else:
             _lib.call("ftl_krp_draw", ctypes.byref(plan), j, self.samples_dev.data_ptr(),
                       self.h_dev.data_ptr(), self.weights_dev.data_ptr(), d_ptr, self.seed,
@@ -196,6 +209,17 @@ class Sampler:
         if d_ptr is None:
             self.counter += 2 * self.N * self.J
         return self.samples_dev, self.h_dev, self.weights_dev
+
+    def _launch_computem(self, b: int, j: int) -> None:
+        # computeM into workspace set b after the trees it reads and after the
+        # descent that last read set b (it does not need the uniforms, so it
+        # is launched before they are copied); the descent waits for _cm_done[b]
+        cm = self._cm_stream
+        cm.wait_event(self._tree_ev)
+        if self._set_free[b] is not None:
+            cm.wait_event(self._set_free[b])
+        _lib.call("ftl_krp_compute_m", ctypes.byref(self._plans[b]), j, int(cm.cuda_stream))
+        self._cm_done[b].record(cm)
 
     def _rows(self, j: int):
         return [k for k in range(self.N) if k != j]

@@ -385,3 +385,54 @@ def test_pinv_square_drops_eigenvalues_like_the_reference(ftl, R):
         ref = O.pinv_square(M, cap, 1e-11)
         assert np.linalg.norm(_pinv_gpu(M, R, R, cap=cap) - ref) <= 1e-9 * np.linalg.norm(ref)
         assert np.linalg.norm(_pinv_gpu(M, R, cap) - ref) <= 1e-9 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("R,j", [(25, 0), (48, 1), (100, 2)])
+def test_sparse_mttkrp_rows_against_numpy(ftl, R, j):
+    """The row-grouped sparse MTTKRP against numpy, 1e-13 relative to the
+    largest entry: queries are the fibers of a random set of nonzeros plus
+    absent fibers, with repeats."""
+    from fast_tensor_leverage_gb300 import _lib
+    rng = np.random.default_rng(300 + R)
+    dims = [70, 50, 40]
+    nnz = 20000
+    flat = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idx = np.stack(np.unravel_index(flat, dims), axis=1).astype(np.uint32)
+    vals = rng.lognormal(0.0, 1.0, size=nnz)
+    sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
+    st = torch.cuda.current_stream().cuda_stream
+    J = 3000
+    keys_all = O.fiber_keys(idx, dims, j)
+    q = np.concatenate([keys_all[rng.integers(0, nnz, size=J - 200)],
+                        rng.integers(0, 2**40, size=200).astype(np.uint64)])
+    keys = torch.from_numpy(q.view(np.int64)).cuda()
+    nb = _lib.ws_bytes("dedup", J)
+    ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    ukeys = torch.empty(J, dtype=torch.int64, device="cuda")
+    urep = torch.empty(J, dtype=torch.int32, device="cuda")
+    ucnt = torch.empty(J, dtype=torch.int32, device="cuda")
+    nu = torch.zeros(1, dtype=torch.int64, device="cuda")
+    _lib.call("ftl_dedup", keys.data_ptr(), J, ws.data_ptr(), nb, ukeys.data_ptr(), urep.data_ptr(),
+              ucnt.data_ptr(), nu.data_ptr(), st)
+    h = torch.from_numpy(rng.normal(size=(J, R))).cuda()
+    w = torch.from_numpy(rng.uniform(0.5, 2.0, size=J)).cuda()
+    rrows, rkeys, rvals = sp.rows[j]
+    mb = _lib.ws_bytes("mttkrp_rows", J, R)
+    mws = torch.empty(mb, dtype=torch.uint8, device="cuda")
+    out = torch.empty((dims[j], R), dtype=torch.float64, device="cuda")
+    _lib.call("ftl_sparse_mttkrp_rows", rrows.data_ptr(), rkeys.data_ptr(), rvals.data_ptr(), sp.nnz,
+              ukeys.data_ptr(), urep.data_ptr(), ucnt.data_ptr(), nu.data_ptr(), J, J, w.data_ptr(),
+              h.data_ptr(), R, mws.data_ptr(), mb, out.data_ptr(), dims[j], st)
+    got = out.cpu().numpy()
+    n = int(nu.item())
+    uk, ur, uc = ukeys.cpu().numpy()[:n].view(np.uint64), urep.cpu().numpy()[:n], ucnt.cpu().numpy()[:n]
+    hh, ww = h.cpu().numpy(), w.cpu().numpy()
+    pos = {int(k): u for u, k in enumerate(uk)}
+    ref = np.zeros((dims[j], R))
+    for z in range(nnz):
+        u = pos.get(int(keys_all[z]))
+        if u is not None:
+            ref[idx[z, j]] += vals[z] * ww[ur[u]] * uc[u] * hh[ur[u]]
+    scale = np.abs(ref).max()
+    assert scale > 0
+    assert np.abs(got - ref).max() <= 1e-13 * scale

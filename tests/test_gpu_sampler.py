@@ -340,3 +340,41 @@ def test_fp32_factor_shadows_give_identical_draws(ftl, R, j):
                   b.weights_dev.data_ptr(), None, 11, 0, st)
         for o in outs:
             assert torch.equal(o[0], b.samples_dev) and torch.equal(o[1], b.h_dev) and torch.equal(o[2], b.weights_dev)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_computem_launched_ahead_matches_fresh_draws(ftl, precision):
+    """After two draws with the same j the sampler launches the next draw's
+    computeM behind the current descent.  Every draw must equal a fresh
+    sampler's draw on the same factors and uniforms: repeated j, a changed j
+    (the launched-ahead result is discarded), and a factor replaced through
+    set_factor between draws (its tree rebuild invalidates it)."""
+    rng = np.random.default_rng(77)
+    N, R, J = 3, 16, 4000
+    dims = [900, 1300, 700]
+    U = [rng.normal(size=(d, R)) for d in dims]
+    s = ftl.Sampler([u.copy() for u in U], J, R, "efficient", precision=precision)
+
+    def fresh(Uc, j, dr):
+        f = ftl.Sampler([u.copy() for u in Uc], J, R, "efficient", precision=precision, overlap_computem=False)
+        out = np.zeros((N, J), dtype=np.uint64)
+        h = np.zeros((J, R))
+        w = np.zeros(J)
+        f.KRPDrawSamples_materialize(j, out, h, w, draws=dr)
+        return out, h, w
+
+    for step, j in enumerate([1, 1, 1, 1, 2, 1, 1, "swap", 1, 1, 0]):
+        if j == "swap":
+            U[0] = rng.normal(size=(dims[0], R))
+            s.set_factor(0, U[0])
+            continue
+        dr = rng.random(2 * N * J)
+        out = np.zeros((N, J), dtype=np.uint64)
+        h = np.zeros((J, R))
+        w = np.zeros(J)
+        s.KRPDrawSamples_materialize(j, out, h, w, draws=dr)
+        ro, rh, rw = fresh(U, j, dr)
+        rows = [k for k in range(N) if k != j]
+        assert (out[rows] == ro[rows]).all(), f"step {step} (j={j}): samples differ"
+        np.testing.assert_array_equal(h, rh)
+        np.testing.assert_array_equal(w, rw)
