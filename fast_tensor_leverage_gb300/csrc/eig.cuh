@@ -65,39 +65,60 @@ __device__ void jacobi_eigen(T *A, T *V, int R, T *csbuf, int *pqbuf, int *flag)
                 pqbuf[2 * tid + 1] = q;
             }
             __syncthreads();
-            // A <- A J and V <- V J (columns p, q of each rotated pair)
-            for (int w = tid; w < half * R; w += nth) {
-                int i = w / R, r = w - i * R;
-                T s = csbuf[2 * i + 1];
-                if (s == T(0)) continue;
-                T c = csbuf[2 * i];
-                int p = pqbuf[2 * i], q = pqbuf[2 * i + 1];
-                T arp = A[r * R + p], arq = A[r * R + q];
-                A[r * R + p] = c * arp - s * arq;
-                A[r * R + q] = s * arp + c * arq;
-                T vrp = V[r * R + p], vrq = V[r * R + q];
-                V[r * R + p] = c * vrp - s * vrq;
-                V[r * R + q] = s * vrp + c * vrq;
-            }
-            __syncthreads();
-            // A <- J^T A (rows p, q)
-            for (int w = tid; w < half * R; w += nth) {
-                int i = w / R, col = w - i * R;
-                T s = csbuf[2 * i + 1];
-                if (s == T(0)) continue;
-                T c = csbuf[2 * i];
-                int p = pqbuf[2 * i], q = pqbuf[2 * i + 1];
-                T apc = A[p * R + col], aqc = A[q * R + col];
-                A[p * R + col] = c * apc - s * aqc;
-                A[q * R + col] = s * apc + c * aqc;
-            }
-            __syncthreads();
-            if (tid < half) {
-                T s = csbuf[2 * tid + 1];
-                if (s != T(0)) {
-                    int p = pqbuf[2 * tid], q = pqbuf[2 * tid + 1];
-                    A[p * R + q] = T(0);
-                    A[q * R + p] = T(0);
+            // A <- J^T A J and V <- V J in one pass: every entry of A lies in
+            // exactly one 2 x 2 block (row pair i, column pair k), rotated by
+            // columns (A J) and then by rows (J^T A), the order of the two
+            // separate passes; the rotated pairs' off-diagonal entries are
+            // then exact zeros.  Indices >= R (the padding pair of odd R,
+            // whose rotation is the identity) have no storage.
+            const int nblk = half * half;
+            for (int w = tid; w < nblk + half * R; w += nth) {
+                if (w < nblk) {
+                    const int i = w / half, k = w - i * half;
+                    const T si = csbuf[2 * i + 1], sk = csbuf[2 * k + 1];
+                    if (si == T(0) && sk == T(0)) continue;
+                    const T ci = csbuf[2 * i], ck = csbuf[2 * k];
+                    const int pi = pqbuf[2 * i], qi = pqbuf[2 * i + 1];
+                    const int pk = pqbuf[2 * k], qk = pqbuf[2 * k + 1];
+                    const bool rq = qi < R, cq = qk < R;
+                    T x00 = A[pi * R + pk];
+                    T x01 = cq ? A[pi * R + qk] : T(0);
+                    T x10 = rq ? A[qi * R + pk] : T(0);
+                    T x11 = (rq && cq) ? A[qi * R + qk] : T(0);
+                    if (sk != T(0)) {
+                        const T t00 = ck * x00 - sk * x01, t01 = sk * x00 + ck * x01;
+                        const T t10 = ck * x10 - sk * x11, t11 = sk * x10 + ck * x11;
+                        x00 = t00;
+                        x01 = t01;
+                        x10 = t10;
+                        x11 = t11;
+                    }
+                    if (si != T(0)) {
+                        const T u00 = ci * x00 - si * x10, u10 = si * x00 + ci * x10;
+                        const T u01 = ci * x01 - si * x11, u11 = si * x01 + ci * x11;
+                        x00 = u00;
+                        x10 = u10;
+                        x01 = u01;
+                        x11 = u11;
+                    }
+                    if (i == k) {
+                        x01 = T(0);
+                        x10 = T(0);
+                    }
+                    A[pi * R + pk] = x00;
+                    if (cq) A[pi * R + qk] = x01;
+                    if (rq) A[qi * R + pk] = x10;
+                    if (rq && cq) A[qi * R + qk] = x11;
+                } else {
+                    const int w2 = w - nblk;
+                    const int k = w2 / R, r = w2 - k * R;
+                    const T sk = csbuf[2 * k + 1];
+                    if (sk == T(0)) continue;
+                    const T ck = csbuf[2 * k];
+                    const int pk = pqbuf[2 * k], qk = pqbuf[2 * k + 1];
+                    const T vrp = V[r * R + pk], vrq = V[r * R + qk];
+                    V[r * R + pk] = ck * vrp - sk * vrq;
+                    V[r * R + qk] = sk * vrp + ck * vrq;
                 }
             }
             __syncthreads();
