@@ -852,24 +852,27 @@ __global__ void residual_thread_kernel(const uint32_t *__restrict__ idx, const d
     }
 }
 
+// *out = sum of the n partials in a fixed order (lane-strided sums, then a
+// fixed shuffle tree): one warp, so the result does not depend on timing.
 __global__ void sum_kernel(const double *__restrict__ partial, int n, double *__restrict__ out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (int k = 0; k < n; ++k) s += partial[k];
-        *out = s;
-    }
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n; k += 32) s += partial[k];
+    s = warp_sum(s);
+    if (threadIdx.x == 0) *out = s;
 }
 
 __global__ void sumsq_partial_kernel(const double *__restrict__ v, int64_t n, double *__restrict__ partial) {
-    __shared__ double red[1024];
+    __shared__ double red[32];
     double acc = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         acc = fma(v[i], v[i], acc);
-    red[threadIdx.x] = acc;
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;
-        for (int t = 0; t < (int)blockDim.x; ++t) s += red[t];
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
         partial[blockIdx.x] = s;
     }
 }

@@ -361,12 +361,16 @@ __global__ void dense_residual_kernel(const VT *__restrict__ T, DenseGeom dg, BB
 }
 
 __global__ void pair_sum_kernel(const double *__restrict__ partial, int nblk, double *__restrict__ out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s0 = 0.0, s1 = 0.0;
-        for (int b = 0; b < nblk; ++b) {
-            s0 += partial[2 * b];
-            s1 += partial[2 * b + 1];
-        }
+    // one warp, fixed order: lane-strided sums, then a shuffle tree
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    double s0 = 0.0, s1 = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += 32) {
+        s0 += partial[2 * b];
+        s1 += partial[2 * b + 1];
+    }
+    s0 = warp_sum(s0);
+    s1 = warp_sum(s1);
+    if (threadIdx.x == 0) {
         out[0] = s0;
         out[1] = s1;
     }
