@@ -33,4 +33,4 @@ int check_launch(const char *what) {
 
 extern "C" const char *ftl_last_error(void) { return ftl::g_last_error; }
 
-extern "C" int ftl_abi_version(void) { return 2; }
+extern "C" int ftl_abi_version(void) { return 3; }
