@@ -599,6 +599,144 @@ __global__ void __launch_bounds__(256, FTL_MTT_MINB)
     }
 }
 
+// Two-phase form of mttkrp_rows_kernel (the same sums in the same order): a
+// warp first probes the whole chunk, UNR batches of 32 nonzeros at a time
+// (their keys, rows, values and first probes all in flight together), and
+// appends the hits (unique index, row, value) to its shared-memory list in
+// nonzero order; it then applies the hits G at a time, loading the G scaled
+// rows together.  The probes and the row loads of a chunk overlap instead of
+// alternating batch by batch.
+constexpr int MTT2_CHUNK = 256;
+#ifndef FTL_MTT2_UNR
+#define FTL_MTT2_UNR 4
+#endif
+#ifndef FTL_MTT2_G
+#define FTL_MTT2_G 8
+#endif
+
+struct HitEntry {
+    int32_t u, row;
+    double val;
+};
+
+template <int CPL, int G, int UNR>
+__global__ void __launch_bounds__(256, 4)
+    mttkrp_rows2_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
+                        const double *__restrict__ rvals, int64_t nnz, const ulonglong2 *__restrict__ pt, int64_t T,
+                        int shift, const double *__restrict__ hs, int R, int Rp, double *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    HitEntry *hits = reinterpret_cast<HitEntry *>(smem_raw) + (threadIdx.x >> 5) * MTT2_CHUNK;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nchunks = (nnz + MTT2_CHUNK - 1) / MTT2_CHUNK;
+    const uint64_t mask = (uint64_t)(T - 1);
+    const unsigned lt = (1u << lane) - 1u;
+    for (int64_t ch = gw; ch < nchunks; ch += nw) {
+        const int64_t z0 = ch * MTT2_CHUNK, z1 = min(nnz, z0 + MTT2_CHUNK);
+        int nh = 0;
+        for (int64_t zb = z0; zb < z1; zb += 32 * UNR) {
+            uint64_t key[UNR], slot[UNR];
+            int32_t row[UNR];
+            double val[UNR];
+            ulonglong2 e[UNR];
+#pragma unroll
+            for (int q = 0; q < UNR; ++q) {
+                const int64_t z = zb + 32 * q + lane;
+                key[q] = kEmpty;
+                row[q] = 0;
+                val[q] = 0.0;
+                if (z < z1) {
+                    key[q] = rkeys[z];
+                    row[q] = rrows[z];
+                    val[q] = rvals[z];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < UNR; ++q) {
+                slot[q] = (key[q] * kFib) >> shift;
+                e[q] = make_ulonglong2(kEmpty, 0);
+                if (key[q] != kEmpty) e[q] = pt[slot[q]];
+            }
+#pragma unroll
+            for (int q = 0; q < UNR; ++q) {
+                int32_t u = -1;
+                if (key[q] != kEmpty) {
+                    uint64_t sl = slot[q];
+                    ulonglong2 x = e[q];
+                    for (int64_t probe = 0; probe < T; ++probe) {
+                        if (x.x == key[q]) {
+                            u = (int32_t)x.y;
+                            break;
+                        }
+                        if (x.x == kEmpty) break;
+                        sl = (sl + 1) & mask;
+                        x = pt[sl];
+                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, u >= 0);
+                if (u >= 0) {
+                    HitEntry &h = hits[nh + __popc(b & lt)];
+                    h.u = u;
+                    h.row = row[q];
+                    h.val = val[q];
+                }
+                nh += __popc(b);
+            }
+        }
+        __syncwarp();
+        double acc[CPL];
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) acc[c] = 0.0;
+        int32_t cur = -1;  // row held in acc (warp-uniform)
+        for (int g0 = 0; g0 < nh; g0 += G) {
+            int32_t hu[G], hrow[G];
+            double hval[G], hv[G][CPL];
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const bool ok = g0 + g < nh;
+                hu[g] = ok ? hits[g0 + g].u : 0;
+                hrow[g] = ok ? hits[g0 + g].row : -1;
+                hval[g] = ok ? hits[g0 + g].val : 0.0;
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+#pragma unroll
+                for (int c = 0; c < CPL; ++c) {
+                    const int col = lane + 32 * c;
+                    hv[g][c] = (g0 + g < nh && col < Rp) ? hs[(int64_t)hu[g] * Rp + col] : 0.0;
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (g0 + g < nh) {
+                    if (hrow[g] != cur) {
+                        if (cur >= 0) {
+#pragma unroll
+                            for (int c = 0; c < CPL; ++c) {
+                                const int col = lane + 32 * c;
+                                if (col < R) atomicAdd(out + (int64_t)cur * R + col, acc[c]);
+                                acc[c] = 0.0;
+                            }
+                        }
+                        cur = hrow[g];
+                    }
+#pragma unroll
+                    for (int c = 0; c < CPL; ++c) acc[c] = fma(hval[g], hv[g][c], acc[c]);
+                }
+            }
+        }
+        if (cur >= 0) {
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+                const int col = lane + 32 * c;
+                if (col < R) atomicAdd(out + (int64_t)cur * R + col, acc[c]);
+            }
+        }
+        __syncwarp();  // the list is rewritten by the next chunk
+    }
+}
+
 // ---------------------------------------------------- range finder (rrf)
 
 // Standard normals of one fiber, two columns per Philox4x32-10 block:
@@ -1030,6 +1168,18 @@ extern "C" int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *ro
     probe_insert_kernel<<<grid_for(J), 256, 0, st>>>(ukeys, num_unique_dev, num_unique, pt, T, shift);
     scaled_unique_rows_kernel<<<grid_for(J * Rp), 256, 0, st>>>(urep, ucnt, w, num_unique_dev, num_unique, h, R, Rp,
                                                                  hs);
+#ifndef FTL_MTT_TWO_PHASE
+#define FTL_MTT_TWO_PHASE 1
+#endif
+    if (FTL_MTT_TWO_PHASE && R <= 32) {
+        const int64_t nch2 = (nnz + MTT2_CHUNK - 1) / MTT2_CHUNK;
+        int blocks2 = (int)std::min<int64_t>((nch2 * 32 + 255) / 256, (int64_t)num_sms() * 32);
+        blocks2 = std::max(blocks2, 1);
+        const size_t smem2 = (size_t)8 * MTT2_CHUNK * sizeof(HitEntry);
+        mttkrp_rows2_kernel<1, FTL_MTT2_G, FTL_MTT2_UNR><<<blocks2, 256, smem2, st>>>(
+            row_idx, row_keys, row_vals, nnz, pt, T, shift, hs, R, Rp, out);
+        return check_launch("mttkrp_rows2_kernel");
+    }
     const int64_t nchunks = (nnz + MTT_CHUNK - 1) / MTT_CHUNK;
     int blocks = (int)std::min<int64_t>((nchunks * 32 + 255) / 256, (int64_t)num_sms() * 32);
     blocks = std::max(blocks, 1);
