@@ -1328,9 +1328,19 @@ extern "C" int ftl_sparse_residual_terms(const uint32_t *idx, const double *vals
     FTL_CHECK_ARG(ws_bytes >= need, "ftl_sparse_residual_terms: workspace too small");
     FactorPtrs fp;
     for (int k = 0; k < FTL_MAX_MODES; ++k) fp.U[k] = k < N ? U_dev[k] : nullptr;
-    const int nblk = num_sms() * 16;
     cudaStream_t st = (cudaStream_t)stream;
     double *part = (double *)workspace;
+    // one wave of resident CTAs for the thread-per-nonzero forms (equal work
+    // per CTA: a grid of a few waves plus a fraction leaves SMs idle at the end)
+    int nblk = num_sms() * 16;
+    if (N >= 2 && N <= 6) {
+        const void *fn = N == 2 ? (const void *)residual_thread_kernel<2> : N == 3 ? (const void *)residual_thread_kernel<3>
+                       : N == 4 ? (const void *)residual_thread_kernel<4> : N == 5 ? (const void *)residual_thread_kernel<5>
+                                                                           : (const void *)residual_thread_kernel<6>;
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 256, 0) == cudaSuccess && occ >= 1)
+            nblk = num_sms() * std::min(occ, 16);
+    }
     switch (N) {
         case 2: residual_thread_kernel<2><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;
         case 3: residual_thread_kernel<3><<<nblk, 256, 0, st>>>(idx, vals, nnz, fp, sigma, R, part); break;

@@ -220,7 +220,12 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
         attr = true;
     }
     int64_t nbatch = (geom.leaf_count + LB - 1) / LB;
-    int grid = (int)std::min<int64_t>(nbatch, (int64_t)sm_count() * 8);
+    // one wave of resident CTAs, each looping over batches: a grid larger
+    // than what fits at once leaves a partial second wave
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_gram_kernel<T>, 256, smem) != cudaSuccess || occ < 1)
+        occ = 1;
+    int grid = (int)std::min<int64_t>(nbatch, (int64_t)sm_count() * occ);
     leaf_gram_kernel<T><<<grid, 256, smem, st>>>(U, n, R, RP, g, LB, G);
     int rc = check_launch("leaf_gram_kernel");
     if (rc) return rc;
