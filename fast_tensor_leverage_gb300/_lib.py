@@ -70,6 +70,12 @@ _SZP = ctypes.POINTER(ctypes.c_size_t)
 SIGNATURES = {
     "ftl_last_error": ([], ctypes.c_char_p),
     "ftl_abi_version": ([], _INT),
+    "ftl_sampler_create": ([_INT, _P, _INT, _I64, _INT, _INT, ctypes.POINTER(_P)], _INT),
+    "ftl_sampler_set_factor": ([_P, _INT, _P, _INT, _P], _INT),
+    "ftl_sampler_update": ([_P, _INT, _P], _INT),
+    "ftl_sampler_factor": ([_P, _INT, ctypes.POINTER(_P)], _INT),
+    "ftl_sampler_draw": ([_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, _P], _INT),
+    "ftl_sampler_destroy": ([_P], _INT),
     "ftl_lowrank_mttkrp_workspace_bytes": ([_INT, _INT, _P], _INT),
     "ftl_lowrank_sampled_mttkrp": ([_P, _P, _INT, _INT, _INT, _P, _I64, _P, _P, _P, _I64, _P, _P, _INT, _P,
                                     ctypes.c_size_t, _P, _I64, _I64, _P], _INT),

@@ -168,6 +168,31 @@ int ftl_krp_sample(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples_dev,
                    double *h_dev, double *weights_dev, const double *draws_dev,
                    uint64_t seed, uint64_t ctr, void *stream);
 
+/* Handle form of the sampler (EfficientKRPSampler, efficient_krp_sampler.hpp:
+ * 32-75 for the state, :209-268 for KRPDrawSamples) for hosts that are not
+ * Python: the handle owns the device factors, Gram trees and workspaces.
+ * Unlike the plan-based entry points, create allocates device memory
+ * (cudaMalloc) and destroy frees it.
+ *   create     : factors zeroed; factor_shadows (FP32 only) keeps FP32 copies
+ *                of the factors for the leaf scans (same results).
+ *   set_factor : copy factor k (dims[k] x R FP64, row-major, host or device)
+ *                and rebuild its tree (Sampler ctor / update_sampler).
+ *   update     : rebuild tree k after the caller wrote the device factor
+ *                returned by ftl_sampler_factor (EfficientKRPSampler::
+ *                update_sampler, :73-75).
+ *   draw       : ftl_krp_draw on the handle's plan (KRPDrawSamples).
+ *   destroy    : waits for the device, frees everything. */
+typedef struct ftl_sampler ftl_sampler;
+int ftl_sampler_create(int N, const int64_t *dims, int R, int64_t J, int prec, int factor_shadows,
+                       ftl_sampler **out);
+int ftl_sampler_set_factor(ftl_sampler *s, int k, const double *U, int U_on_host, void *stream);
+int ftl_sampler_update(ftl_sampler *s, int k, void *stream);
+int ftl_sampler_factor(const ftl_sampler *s, int k, double **U_dev);
+int ftl_sampler_draw(ftl_sampler *s, uint32_t j, uint64_t *samples_dev, double *h_dev,
+                     double *weights_dev, const double *draws_dev, uint64_t seed, uint64_t ctr,
+                     void *stream);
+int ftl_sampler_destroy(ftl_sampler *s);
+
 /* ------------------------------------------------ sparse tensors and CP-ALS */
 
 /* Fiber keys: keys_out[i] = mixed-radix number of the indices of every mode

@@ -79,3 +79,14 @@ def test_plan_validation_rejects_bad_plans():
     plan.N = 0
     with pytest.raises(_lib.FTLError):
         _lib.call("ftl_krp_compute_m", ctypes.byref(plan), 0, None)
+
+
+def test_sampler_handle_rejects_bad_shapes_without_touching_the_device():
+    """ftl_sampler_create validates its arguments before any allocation."""
+    h = ctypes.c_void_p(12345)
+    dims = (ctypes.c_int64 * 3)(10, 20, 30)
+    L = _lib.lib()
+    for N, R, J, prec in [(0, 8, 10, 0), (3, 0, 10, 0), (3, 8, 0, 0), (3, 8, 10, 7), (3, 200, 10, 0)]:
+        assert L.ftl_sampler_create(N, dims, R, J, prec, 0, ctypes.byref(h)) == 1
+        assert h.value is None
+    assert L.ftl_sampler_destroy(None) == 0

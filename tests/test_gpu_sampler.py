@@ -378,3 +378,52 @@ def test_computem_launched_ahead_matches_fresh_draws(ftl, precision):
         assert (out[rows] == ro[rows]).all(), f"step {step} (j={j}): samples differ"
         np.testing.assert_array_equal(h, rh)
         np.testing.assert_array_equal(w, rw)
+
+
+@pytest.mark.parametrize("precision,shadows", [("fp64", 0), ("fp32", 0), ("fp32", 1)])
+def test_sampler_handle_matches_python_sampler(ftl, precision, shadows):
+    """The handle API (ftl_sampler_create / set_factor / draw / destroy, for
+    hosts that are not Python) gives the Python Sampler's draws bit for bit:
+    factors copied from host arrays, injected uniforms, j excluded and none
+    excluded; then factor 1 replaced through the device pointer and
+    ftl_sampler_update."""
+    import ctypes
+    from fast_tensor_leverage_gb300 import _lib
+    rng = np.random.default_rng(404)
+    N, R, J = 3, 24, 3000
+    dims = [700, 1100, 90]
+    U = [np.ascontiguousarray(rng.normal(size=(d, R))) for d in dims]
+    prec = _lib.PREC[precision]
+    st = torch.cuda.current_stream().cuda_stream
+    h = ctypes.c_void_p()
+    dims_c = (ctypes.c_int64 * N)(*dims)
+    _lib.call("ftl_sampler_create", N, dims_c, R, J, prec, shadows, ctypes.byref(h))
+    try:
+        for k in range(N):
+            _lib.call("ftl_sampler_set_factor", h, k, U[k].ctypes.data, 1, st)
+        for step, j in enumerate([1, 3, 1]):
+            if step == 2:
+                U[1] = np.ascontiguousarray(rng.normal(size=(dims[1], R)))
+                # write the handle's device factor directly, then rebuild its tree
+                dptr = ctypes.c_void_p()
+                _lib.call("ftl_sampler_factor", h, 1, ctypes.byref(dptr))
+                dev = torch.from_numpy(U[1]).cuda()
+                torch.cuda.synchronize()
+                view = type("DevView", (), {"__cuda_array_interface__": {
+                    "shape": (dims[1], R), "typestr": "<f8", "data": (dptr.value, False), "version": 3}})()
+                torch.as_tensor(view, device="cuda").copy_(dev)
+                _lib.call("ftl_sampler_update", h, 1, st)
+            dr = rng.random(2 * N * J)
+            drd = torch.from_numpy(dr).cuda()
+            smp = torch.zeros((N, J), dtype=torch.int64, device="cuda")
+            hh = torch.empty((J, R), dtype=torch.float64, device="cuda")
+            ww = torch.empty(J, dtype=torch.float64, device="cuda")
+            _lib.call("ftl_sampler_draw", h, j, smp.data_ptr(), hh.data_ptr(), ww.data_ptr(), drd.data_ptr(),
+                      0, 0, st)
+            ref = ftl.Sampler([u.copy() for u in U], J, R, "efficient", precision=precision, overlap_computem=False)
+            rs, rh, rw = ref.draw(j, dr)
+            rows = [k for k in range(N) if k != j]
+            assert torch.equal(smp[rows], rs[rows]), f"step {step}: samples differ"
+            assert torch.equal(hh, rh) and torch.equal(ww, rw)
+    finally:
+        _lib.call("ftl_sampler_destroy", h)
