@@ -76,6 +76,20 @@ SIGNATURES = {
     "ftl_sampler_factor": ([_P, _INT, ctypes.POINTER(_P)], _INT),
     "ftl_sampler_draw": ([_P, ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_uint64, ctypes.c_uint64, _P], _INT),
     "ftl_sampler_destroy": ([_P], _INT),
+    "ftl_sparse_create": ([_P, _P, _I64, _INT, _P, _INT, _P, ctypes.POINTER(_P)], _INT),
+    "ftl_sparse_normsq": ([_P, ctypes.POINTER(ctypes.c_double)], _INT),
+    "ftl_sparse_destroy": ([_P], _INT),
+    "ftl_als_create": ([_P, _INT, _I64, _INT, ctypes.c_uint64, ctypes.POINTER(_P)], _INT),
+    "ftl_als_set_factor": ([_P, _INT, _P, _INT, _P], _INT),
+    "ftl_als_set_sigma": ([_P, _P, _INT, _P], _INT),
+    "ftl_als_factor": ([_P, _INT, ctypes.POINTER(_P)], _INT),
+    "ftl_als_sigma": ([_P, ctypes.POINTER(_P)], _INT),
+    "ftl_als_samples": ([_P, ctypes.POINTER(_P)], _INT),
+    "ftl_als_renormalize": ([_P, _INT, _P], _INT),
+    "ftl_als_init_rrf": ([_P, ctypes.c_uint64, _P], _INT),
+    "ftl_als_update": ([_P, _INT, _INT, _INT, _P, _P], _INT),
+    "ftl_als_fit": ([_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _P], _INT),
+    "ftl_als_destroy": ([_P], _INT),
     "ftl_lowrank_mttkrp_workspace_bytes": ([_INT, _INT, _P], _INT),
     "ftl_lowrank_sampled_mttkrp": ([_P, _P, _INT, _INT, _INT, _P, _I64, _P, _P, _P, _I64, _P, _P, _INT, _P,
                                     ctypes.c_size_t, _P, _I64, _I64, _P], _INT),

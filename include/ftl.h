@@ -278,6 +278,46 @@ int ftl_sparse_mttkrp_rows(const int32_t *row_idx, const uint64_t *row_keys,
 int ftl_solve_rows(const double *B_dev, const double *pinv_dev, int64_t I, int R, double *U_dev,
                    void *stream);
 
+/* Handle form of the sparse tensor and of the randomized CP-ALS for hosts
+ * that are not Python (SparseTensor + SortIdxLookup, sparse_tensor.hpp:46-77,
+ * sort_lookup.hpp:33-60; ALS initialize_ds_als / execute_ds_als_update,
+ * als.hpp:39-220; execute_rrf, sparse_tensor.hpp:84-92; the exact fit,
+ * sparse_tensor.hpp:117-119 and tensors.py:41-53).  Creating allocates device
+ * memory; destroy frees it.
+ *   ftl_sparse_create : copies idx (nnz x N uint32, row-major) and vals
+ *                       (host or device), sorts the nonzeros by each mode's
+ *                       index (stable) with their fiber keys, and computes
+ *                       the squared norm (the call waits for the device).
+ *   ftl_als_create    : an ALS over the tensor's dims with rank R and J samples
+ *                       per update; owns a sampler handle (the factors) and
+ *                       every buffer an update needs; sigma starts at ones.
+ *   ftl_als_set_factor / set_sigma : initial factors (tree rebuilt) and sigma.
+ *   ftl_als_init_rrf  : range-finder factors (execute_rrf), then
+ *                       ftl_als_renormalize(-1).
+ *   ftl_als_renormalize : column norms of factor j (-1: all), sigma = the
+ *                       norms (product over modes for -1), trees rebuilt.
+ *   ftl_als_update    : one sampled update of mode j; draws_dev (2N x J
+ *                       uniforms) or NULL for the handle's Philox stream.
+ *   ftl_als_fit       : 1 - ||X - model|| / ||X|| and ||X - model||^2 (waits). */
+typedef struct ftl_sparse ftl_sparse;
+typedef struct ftl_als ftl_als;
+int ftl_sparse_create(const uint32_t *idx, const double *vals, int64_t nnz, int N, const int64_t *dims,
+                      int on_host, void *stream, ftl_sparse **out);
+int ftl_sparse_normsq(const ftl_sparse *X, double *out);
+int ftl_sparse_destroy(ftl_sparse *X);
+int ftl_als_create(const ftl_sparse *X, int R, int64_t J, int prec, uint64_t seed, ftl_als **out);
+int ftl_als_set_factor(ftl_als *A, int k, const double *U, int on_host, void *stream);
+int ftl_als_set_sigma(ftl_als *A, const double *sigma, int on_host, void *stream);
+int ftl_als_factor(const ftl_als *A, int k, double **U_dev);
+int ftl_als_sigma(const ftl_als *A, double **sigma_dev);
+int ftl_als_samples(const ftl_als *A, uint64_t **samples_dev);
+int ftl_als_renormalize(ftl_als *A, int j, void *stream);
+int ftl_als_init_rrf(ftl_als *A, uint64_t seed, void *stream);
+int ftl_als_update(ftl_als *A, int j, int renormalize, int update_sampler, const double *draws_dev,
+                   void *stream);
+int ftl_als_fit(ftl_als *A, double *fit, double *residual_normsq, void *stream);
+int ftl_als_destroy(ftl_als *A);
+
 /* Column norms of U (I x R) with norms <= 1e-7 replaced by 1, and (apply != 0)
  * U *= 1/norms (the reference divides; this differs by at most one rounding).  Replaces LowRankTensor::renormalize_columns for one factor,
  * cpp_ext/low_rank_tensor.hpp:203-247. */

@@ -436,3 +436,96 @@ def test_sparse_mttkrp_rows_against_numpy(ftl, R, j):
     scale = np.abs(ref).max()
     assert scale > 0
     assert np.abs(got - ref).max() <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("name", als_cases())
+def test_als_handle_matches_reference_golden(ftl, name):
+    """The native handle path (ftl_sparse_create, ftl_als_create, set_factor,
+    set_sigma, ftl_als_update with injected uniforms, ftl_als_fit) against the
+    reference's recorded ALS: the tolerances of the Python-path test."""
+    import ctypes
+    from fast_tensor_leverage_gb300 import _lib
+    c = load_als(name)
+    N, R, J = c["N"], c["R"], c["J"]
+    st = torch.cuda.current_stream().cuda_stream
+    idx = np.ascontiguousarray(c["idx"], dtype=np.uint32)
+    vals = np.ascontiguousarray(c["vals"], dtype=np.float64)
+    dims = (ctypes.c_int64 * N)(*c["dims"])
+    X, A = ctypes.c_void_p(), ctypes.c_void_p()
+    _lib.call("ftl_sparse_create", idx.ctypes.data, vals.ctypes.data, idx.shape[0], N, dims, 1, st, ctypes.byref(X))
+    try:
+        nsq = ctypes.c_double()
+        _lib.call("ftl_sparse_normsq", X, ctypes.byref(nsq))
+        assert abs(nsq.value - c["normsq"]) <= 1e-12 * c["normsq"]
+        _lib.call("ftl_als_create", X, R, J, 0, 1, ctypes.byref(A))
+        for k in range(N):
+            u0 = np.ascontiguousarray(c["U0"][k])
+            _lib.call("ftl_als_set_factor", A, k, u0.ctypes.data, 1, st)
+        s0 = np.ascontiguousarray(c["sigma0"])
+        _lib.call("ftl_als_set_sigma", A, s0.ctypes.data, 1, st)
+
+        def dev_view(ptr, shape, typestr):
+            v = type("V", (), {"__cuda_array_interface__": {
+                "shape": shape, "typestr": typestr, "data": (ptr, False), "version": 3}})()
+            return torch.as_tensor(v, device="cuda")
+
+        sp_ptr, sg_ptr = ctypes.c_void_p(), ctypes.c_void_p()
+        _lib.call("ftl_als_samples", A, ctypes.byref(sp_ptr))
+        _lib.call("ftl_als_sigma", A, ctypes.byref(sg_ptr))
+        samples_t = dev_view(sp_ptr.value, (N, J), "<i8")
+        sigma_t = dev_view(sg_ptr.value, (R,), "<f8")
+        for u, upd in enumerate(c["updates"]):
+            j = upd["j"]
+            dr = torch.from_numpy(upd["draws"]).cuda()
+            _lib.call("ftl_als_update", A, j, 1, 1, dr.data_ptr(), st)
+            torch.cuda.synchronize()
+            samples = samples_t.cpu().numpy().view(np.uint64)
+            rows = [k for k in range(N) if k != j]
+            assert np.array_equal(samples[rows], upd["samples"][rows]), f"update {u}: samples differ"
+            up = ctypes.c_void_p()
+            _lib.call("ftl_als_factor", A, j, ctypes.byref(up))
+            Uj = dev_view(up.value, (c["dims"][j], R), "<f8").cpu().numpy()
+            np.testing.assert_allclose(Uj, upd["U"], rtol=0, atol=1e-9 * np.abs(upd["U"]).max())
+            np.testing.assert_allclose(sigma_t.cpu().numpy(), upd["sigma"], rtol=1e-9)
+            if (u + 1) % N == 0:
+                fit, resid = ctypes.c_double(), ctypes.c_double()
+                _lib.call("ftl_als_fit", A, ctypes.byref(fit), ctypes.byref(resid), st)
+                ref = c["resid"][u // N]
+                np.testing.assert_allclose(resid.value, ref, rtol=1e-9)
+                fit_ref = 1 - np.sqrt(ref / c["normsq"])
+                assert abs(fit.value - fit_ref) <= 1e-6 * abs(fit_ref)
+    finally:
+        _lib.call("ftl_als_destroy", A)
+        _lib.call("ftl_sparse_destroy", X)
+
+
+def test_als_handle_rrf_mixed_precision_runs(ftl):
+    """Range-finder initialisation and Philox-driven mixed-precision updates
+    through the handle: the fit is finite and the sweep improves on the
+    initial model."""
+    import ctypes
+    from fast_tensor_leverage_gb300 import _lib
+    rng = np.random.default_rng(123)
+    dims = [300, 200, 100]
+    nnz = 30000
+    flat = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idx = np.ascontiguousarray(np.stack(np.unravel_index(flat, dims), axis=1).astype(np.uint32))
+    vals = np.log1p(rng.lognormal(size=nnz))
+    st = torch.cuda.current_stream().cuda_stream
+    X, A = ctypes.c_void_p(), ctypes.c_void_p()
+    _lib.call("ftl_sparse_create", idx.ctypes.data, vals.ctypes.data, nnz, 3, (ctypes.c_int64 * 3)(*dims), 1, st,
+              ctypes.byref(X))
+    try:
+        _lib.call("ftl_als_create", X, 10, 4096, 1, 99, ctypes.byref(A))
+        _lib.call("ftl_als_init_rrf", A, 5, st)
+        f0 = ctypes.c_double()
+        _lib.call("ftl_als_fit", A, ctypes.byref(f0), None, st)
+        for _ in range(3):
+            for j in range(3):
+                _lib.call("ftl_als_update", A, j, 1, 1, None, st)
+        f1 = ctypes.c_double()
+        _lib.call("ftl_als_fit", A, ctypes.byref(f1), None, st)
+        assert np.isfinite(f1.value) and f1.value > f0.value
+    finally:
+        _lib.call("ftl_als_destroy", A)
+        _lib.call("ftl_sparse_destroy", X)
