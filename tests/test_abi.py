@@ -90,3 +90,20 @@ def test_sampler_handle_rejects_bad_shapes_without_touching_the_device():
         assert L.ftl_sampler_create(N, dims, R, J, prec, 0, ctypes.byref(h)) == 1
         assert h.value is None
     assert L.ftl_sampler_destroy(None) == 0
+
+
+def test_sparse_and_als_handles_reject_bad_arguments_without_touching_the_device():
+    """ftl_sparse_create / ftl_als_create validate before any allocation or copy."""
+    L = _lib.lib()
+    X = ctypes.c_void_p(7)
+    idx = (ctypes.c_uint32 * 6)(0, 0, 1, 1, 2, 2)
+    vals = (ctypes.c_double * 3)(1.0, 2.0, 3.0)
+    dims = (ctypes.c_int64 * 2)(3, 3)
+    for nnz, N in [(0, 2), (3, 1), (3, 17)]:
+        assert L.ftl_sparse_create(idx, vals, nnz, N, dims, 1, None, ctypes.byref(X)) == 1
+        assert X.value is None
+    bad_dims = (ctypes.c_int64 * 2)(3, 0)
+    assert L.ftl_sparse_create(idx, vals, 3, 2, bad_dims, 1, None, ctypes.byref(X)) == 1
+    A = ctypes.c_void_p(9)
+    assert L.ftl_als_create(None, 8, 100, 0, 1, ctypes.byref(A)) == 1
+    assert L.ftl_sparse_destroy(None) == 0 and L.ftl_als_destroy(None) == 0
