@@ -619,8 +619,11 @@ struct HitEntry {
     double val;
 };
 
+#ifndef FTL_MTT2_MINB
+#define FTL_MTT2_MINB 4
+#endif
 template <int CPL, int G, int UNR>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, FTL_MTT2_MINB)
     mttkrp_rows2_kernel(const int32_t *__restrict__ rrows, const uint64_t *__restrict__ rkeys,
                         const double *__restrict__ rvals, int64_t nnz, const ulonglong2 *__restrict__ pt, int64_t T,
                         int shift, const double *__restrict__ hs, int R, int Rp, double *__restrict__ out) {
