@@ -228,28 +228,27 @@ __global__ void computem_eig_kernel(CMParams p) {
     const int S = node_stride(R, sizeof(T));
     T *G = (T *)p.eig_G + (size_t)k * (2 * R - 1) * S;
     const DGeom g = p.eig;
+    // (an eigen tree has 2R - 1 <= 255 nodes of S <= 8256 values: 32-bit indexing)
     const int leaf_count = R;
-    for (int e = tid; e < leaf_count * S; e += nth) {
-        int u = e / S, pe = e - u * S;
-        T v = T(0);
-        if (pe < P) {
-            int a = 0, rem = pe;
-            while (rem >= R - a) {
-                rem -= R - a;
-                ++a;
-            }
-            int b = a + rem;
-            v = (T)W[u * R + a] * (T)W[u * R + b];
-        }
-        G[leaf_node(g, u) * S + pe] = v;
+    // leaves: one work item per (leaf u, packed row a), the row's entries
+    // b = a..R-1 contiguous in the packed layout; then the node padding
+    for (int w = tid; w < leaf_count * R; w += nth) {
+        const int u = w / R, a = w - u * R;
+        T *row = G + (int)leaf_node(g, u) * S + packed_row_offset(a, R);
+        const T wa = (T)W[u * R + a];
+        for (int b = a; b < R; ++b) row[b - a] = wa * (T)W[u * R + b];
+    }
+    for (int w = tid; w < leaf_count * (S - P); w += nth) {
+        const int u = w / (S - P);
+        G[(int)leaf_node(g, u) * S + P + (w - u * (S - P))] = T(0);
     }
     __syncthreads();
-    int64_t start = g.nodes_upto_lfill - ((g.nodes_upto_lfill + 1) / 2);  // nodes_before_lfill
-    int64_t end = g.node_count - leaf_count;
+    int start = (int)(g.nodes_upto_lfill - ((g.nodes_upto_lfill + 1) / 2));  // nodes_before_lfill
+    int end = (int)(g.node_count - leaf_count);
     while (true) {
-        for (int64_t e = tid; e < (end - start) * S; e += nth) {
-            int64_t c = start + e / S;
-            int pe = (int)(e % S);
+        for (int e = tid; e < (end - start) * S; e += nth) {
+            const int cc = e / S;
+            const int c = start + cc, pe = e - cc * S;
             G[c * S + pe] = G[(2 * c + 1) * S + pe] + G[(2 * c + 2) * S + pe];
         }
         __syncthreads();
@@ -257,8 +256,8 @@ __global__ void computem_eig_kernel(CMParams p) {
         end = start;
         start = (start + 1) / 2 - 1;
     }
-    for (int64_t e = tid; e < (int64_t)(2 * R - 1) * S; e += nth) {
-        int pe = (int)(e % S);
+    for (int e = tid; e < (2 * R - 1) * S; e += nth) {
+        const int pe = e % S;
         if (pe < P) G[e] = G[e] * (T)root_at(p, k, pe);
     }
 }
