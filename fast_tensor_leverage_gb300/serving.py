@@ -188,7 +188,7 @@ class ServingEngine:
         self._streams = [torch.cuda.Stream(self.device) for _ in range(self.max_active)]
         if reserve:
             # Map the whole budget once: later requests split cached blocks
-            # instead of asking the driver for memory while other requests
+            # instead of asking the CUDA driver (cudaMalloc) for memory while other requests
             # run (large device allocations can synchronise the device).
             with torch.cuda.stream(self._setup_stream):
                 block = torch.empty(self.budget, dtype=torch.uint8, device=self.device)
