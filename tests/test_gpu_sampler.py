@@ -427,3 +427,34 @@ def test_sampler_handle_matches_python_sampler(ftl, precision, shadows):
             assert torch.equal(hh, rh) and torch.equal(ww, rw)
     finally:
         _lib.call("ftl_sampler_destroy", h)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sketched_least_squares_residual_ratio(ftl, precision):
+    """The reference's accuracy benchmark (benchmarks/accuracy_tests_residual.py:
+    21-79) restated as an assertion: solve min ||A x - b|| over the KRP A of
+    three 40 x 8 factors (64,000 rows) from J = 4,000 leverage samples with
+    their importance weights, and compare the full residual with the exact
+    least-squares residual: the ratio is 1 + O(R / J); the oracle's samples
+    give 1.0001 here, uniform sampling of the same size 1.007."""
+    rng = np.random.default_rng(2024)
+    N, I, R, J = 3, 40, 8, 4000
+    U = [rng.normal(size=(I, R)) for _ in range(N)]
+    for u in U:
+        heavy = rng.choice(I, size=2, replace=False)
+        u[heavy] *= 30.0
+    A = np.einsum("ir,jr,kr->ijkr", *U).reshape(-1, R)
+    b = A @ rng.normal(size=R) + 0.5 * rng.normal(size=A.shape[0]) * np.abs(A).mean()
+    x_exact = np.linalg.lstsq(A, b, rcond=None)[0]
+    r_exact = np.linalg.norm(A @ x_exact - b)
+    s = ftl.Sampler([u.copy() for u in U], J, R, "efficient", precision=precision, seed=5)
+    samples = np.zeros((N, J), dtype=np.uint64)
+    h = np.zeros((J, R))
+    w = np.zeros(J)
+    s.KRPDrawSamples_materialize(N + 1, samples, h, w)
+    rows = (samples[0].astype(np.int64) * I + samples[1].astype(np.int64)) * I + samples[2].astype(np.int64)
+    np.testing.assert_allclose(h, A[rows], rtol=1e-12, atol=1e-12 * np.abs(A).max())
+    sw = np.sqrt(w)
+    x_s = np.linalg.lstsq(sw[:, None] * h, sw * b[rows], rcond=None)[0]
+    ratio = np.linalg.norm(A @ x_s - b) / r_exact
+    assert ratio < 1.01, ratio
