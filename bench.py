@@ -260,9 +260,10 @@ def run_ours(args, ws, rank, local):
         if ws > 1:
             torch.distributed.barrier()
 
-    def time_draws(sampler, steps, warmup, clocks=None):
+    def time_draws(sampler, steps, warmup, clocks=None, jj=None):
+        jj = j if jj is None else jj
         for _ in range(warmup):
-            sampler.draw(j)
+            sampler.draw(jj)
         barrier()
         torch.cuda.synchronize(dev)
         if clocks:
@@ -272,7 +273,7 @@ def run_ours(args, ws, rank, local):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(st)
         for _ in range(steps):
-            sampler.draw(j)
+            sampler.draw(jj)
         e1.record(st)
         torch.cuda.synchronize(dev)
         barrier()
@@ -327,6 +328,10 @@ def run_ours(args, ws, rank, local):
            "d2h_bytes_per_step": N * J * 8 + J * R * 8 + J * 8,
            "api": "Sampler.KRPDrawSamples_materialize(j, samples, h_out, weights_out, draws=pinned host uniforms)"}
 
+    # the other C2 variant: one mode excluded (j = 0, two descents per sample)
+    ms_j0, _ = time_draws(s, max(20, args.steps // 5), max(3, args.warmup // 4), jj=0)
+    one_excluded = {"j": 0, "value": whole_job_rate(ws, J, ms_j0 / 1e3), "ms_per_step": ms_j0}
+
     # the plain FP64 GPU path on the same workload, for the mixed/FP64 ratio
     fp64 = None
     if args.precision == "fp32" and not args.no_fp64_arm:
@@ -365,6 +370,7 @@ def run_ours(args, ws, rank, local):
                      "algorithmic_bytes_per_launch": alg},
         "clocks": clk,
         "cpu_baseline": cpu,
+        "one_mode_excluded": one_excluded,
     }
     if fp64 is not None:
         line["fp64_path"] = fp64
