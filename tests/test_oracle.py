@@ -97,3 +97,26 @@ def test_oracle_matches_live_reference(N, dims, R, J, j, seed):
     rows = included_rows(N, j if j < N else N + 1)
     assert np.array_equal(out[rows], ref[rows])
     assert np.array_equal(o.h, hr)
+
+
+def test_oracle_sketched_least_squares_residual_ratio():
+    """The reference's accuracy benchmark (benchmarks/accuracy_tests_residual.py:
+    21-79) as an assertion on the oracle: least squares over a 64,000-row KRP
+    solved from J = 4,000 leverage samples with their weights leaves a
+    residual within 1% of the exact one (the GPU test asserts the same on the
+    device's samples)."""
+    rng = np.random.default_rng(2024)
+    N, I, R, J = 3, 40, 8, 4000
+    U = [rng.normal(size=(I, R)) for _ in range(N)]
+    for u in U:
+        heavy = rng.choice(I, size=2, replace=False)
+        u[heavy] *= 30.0
+    A = np.einsum("ir,jr,kr->ijkr", *U).reshape(-1, R)
+    b = A @ rng.normal(size=R) + 0.5 * rng.normal(size=A.shape[0]) * np.abs(A).mean()
+    r_exact = np.linalg.norm(A @ np.linalg.lstsq(A, b, rcond=None)[0] - b)
+    o = O.OracleKRPSampler(U, J, R)
+    smp = o.draw(N + 1, np.random.default_rng(1).random(2 * N * J))
+    rows = (smp[0].astype(np.int64) * I + smp[1].astype(np.int64)) * I + smp[2].astype(np.int64)
+    sw = np.sqrt(o.weights)
+    x_s = np.linalg.lstsq(sw[:, None] * A[rows], sw * b[rows], rcond=None)[0]
+    assert np.linalg.norm(A @ x_s - b) / r_exact < 1.01
