@@ -125,6 +125,26 @@ class LowRankTensor:
         s = np.ascontiguousarray(np.asarray(sigma_in, dtype=np.float64).reshape(-1)[: self.R])
         self.sigma_dev.copy_(torch.from_numpy(s))
 
+    # ---------------------------------------------------- perturbation
+    def multiply_random_factor_entries(self, rho: float, A: float, seed: int | None = None) -> None:
+        """Multiply each factor entry by A with probability rho, independently
+        (LowRankTensor::multiply_random_factor_entries,
+        low_rank_tensor.hpp:289-303, which draws from an unseeded generator;
+        here `seed` makes it reproducible, None draws a fresh one).  Like the
+        reference it does not touch a sampler built on these factors: call
+        its update_sampler afterwards."""
+        import secrets
+        if not 0.0 <= float(rho) <= 1.0:
+            raise ValueError(f"rho={rho} outside [0, 1]")
+        g = torch.Generator(device=self.device)
+        g.manual_seed(secrets.randbits(63) if seed is None else int(seed))
+        for k in range(self.N):
+            hit = torch.rand(self.U_dev[k].shape, generator=g, device=self.device, dtype=torch.float64) < float(rho)
+            self.U_dev[k][hit] *= float(A)
+        self._normsq = None if not self.is_static else self._chain_sum_self()
+        if self.sync_host:
+            self.sync_host_copies()
+
     # ------------------------------------------------------ renormalise
     def renormalize_columns(self, j: int) -> None:
         """Divide the columns of factor j (j = -1: every factor) by their

@@ -529,3 +529,26 @@ def test_als_handle_rrf_mixed_precision_runs(ftl):
     finally:
         _lib.call("ftl_als_destroy", A)
         _lib.call("ftl_sparse_destroy", X)
+
+
+def test_multiply_random_factor_entries(ftl):
+    """LowRankTensor.multiply_random_factor_entries(rho, A): each entry
+    scaled by A with probability rho (low_rank_tensor.hpp:289-303), host
+    arrays mirrored, reproducible with a seed."""
+    rng = np.random.default_rng(8)
+    U = [rng.normal(size=(5000, 8)) for _ in range(3)]
+    orig = [u.copy() for u in U]
+    lr = ftl.LowRankTensor(8, U)
+    lr.multiply_random_factor_entries(0.01, 10.0, seed=3)
+    changed = 0
+    for u, o in zip(U, orig):
+        hit = u != o
+        np.testing.assert_array_equal(u[hit], o[hit] * 10.0)
+        changed += int(hit.sum())
+    frac = changed / (3 * 5000 * 8)
+    assert 0.008 < frac < 0.012, frac
+    U2 = [o.copy() for o in orig]
+    lr2 = ftl.LowRankTensor(8, U2)
+    lr2.multiply_random_factor_entries(0.01, 10.0, seed=3)
+    for a, b in zip(U, U2):
+        np.testing.assert_array_equal(a, b)
