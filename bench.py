@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--R", type=int, default=32)
     ap.add_argument("--J", type=int, default=50000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="sampling", choices=["sampling", "als", "serve", "lowrank"],
+    ap.add_argument("--workload", default="sampling",
+                    choices=["sampling", "als", "serve", "lowrank", "launcher-check"],
                     help="als: randomized CP-ALS on the synthetic sparse tensor (seconds per sweep); "
                          "serve: Poisson stream of sampling and CP-ALS requests (p50/p99 latency)")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
@@ -87,6 +88,34 @@ def max_over_ranks(x: float, ws: int, device=None) -> float:
     t = torch.tensor([float(x)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def free_port() -> int:
+    import socket
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def spawn_command(argv: list[str], nproc: int, port: int | None = None) -> list[str]:
+    """The launch of this script as `nproc` ranks on one node (one process
+    per GPU, RANK / LOCAL_RANK / WORLD_SIZE set by torch.distributed.run,
+    rendezvous on 127.0.0.1)."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={nproc}",
+            "--master-addr", "127.0.0.1", "--master-port", str(port or free_port()),
+            str(Path(__file__).resolve()), *argv]
+
+
+def launcher_check(ws: int, rank: int, local: int):
+    """The multi-rank plumbing without a GPU: gloo ranks agree on the max
+    over ranks and on the whole-job rate (used by the CPU tests)."""
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    slowest = max_over_ranks(1.0 + rank, ws)
+    line = {"n_gpus": ws, "rank": rank, "local_rank": local, "max_over_ranks": slowest,
+            "whole_job_rate": whole_job_rate(ws, 100.0, slowest), "seeds": replica_seeds(rank)}
+    dist.destroy_process_group()
+    return line if rank == 0 else None
 
 
 def replica_seeds(rank: int) -> dict:
@@ -217,17 +246,33 @@ def algorithmic_bytes(samples, dims, R, J, N, j, prec_bytes, shadow=False):
     return total
 
 
+def source_tag() -> str:
+    """Hash of the descent kernel's sources; a committed ncu summary carries
+    the tag of the sources it was captured from, so a stale one is detected."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in ("descent.cuh", "krp_draw.cu", "ftl_common.cuh"):
+        h.update((REPO / "fast_tensor_leverage_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
 def read_traffic(precision):
-    """dram bytes per launch of the descent kernel from the committed ncu
-    summary (profiles/krp_draw_kernel_*.md, line 'traffic_bytes_per_launch')."""
+    """DRAM bytes per C2 descent launch from the committed ncu summary
+    (profiles/krp_draw_kernel_<precision>_*.md, lines 'traffic_bytes_per_launch:'
+    and 'source_tag:').  None when no summary matches the current sources."""
+    tag = source_tag()
     for f in sorted((REPO / "profiles").glob(f"krp_draw_kernel_{precision}_*.md")):
+        vals = {}
         for line in f.read_text().splitlines():
-            if line.strip().startswith("traffic_bytes_per_launch:"):
-                try:
-                    return float(line.split(":", 1)[1].strip().split()[0])
-                except ValueError:
-                    return None
-    return None
+            for key in ("traffic_bytes_per_launch:", "source_tag:"):
+                if line.strip().startswith(key):
+                    vals[key] = line.split(":", 1)[1].strip().split()[0]
+        if vals.get("source_tag:") == tag and "traffic_bytes_per_launch:" in vals:
+            try:
+                return float(vals["traffic_bytes_per_launch:"]), f.name
+            except ValueError:
+                pass
+    return None, f"no ncu summary for source tag {tag}"
 
 
 def measured_peak():
@@ -236,6 +281,44 @@ def measured_peak():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def binom_upper(k: int, n: int, z: float = 1.96) -> float:
+    """Wilson upper bound of a binomial proportion (k of n)."""
+    if n == 0:
+        return 1.0
+    p = k / n
+    den = 1 + z * z / n
+    c = p + z * z / (2 * n)
+    r = z * ((p * (1 - p) / n + z * z / (4 * n * n)) ** 0.5)
+    return (c + r) / den
+
+
+def small_krp_tv(ftl, precision, seed=2023, N=3, I=8, R=4, J=1 << 20, reps=64):
+    """Total-variation distance between 2^26 draws of the sampler and the
+    exact leverage distribution of a 512-row KRP (1% of entries x10), the
+    exact scores by brute force in FP64 (K pinv(K^T K) K^T on the
+    materialised KRP), with the sampling-noise level of that many draws."""
+    import torch
+    rng = np.random.default_rng(seed)
+    U = [rng.normal(size=(I, R)) for _ in range(N)]
+    for u in U:
+        u[rng.random(u.shape) < 0.01] *= 10.0
+    K = np.ones((1, R))
+    for u in U:
+        K = (K[:, None, :] * u[None, :, :]).reshape(-1, R)
+    lev = np.einsum("ij,jk,ik->i", K, np.linalg.pinv(K.T @ K), K)
+    p = lev / lev.sum()
+    s = ftl.Sampler(U, J, R, "efficient", precision=precision, seed=99)
+    counts = torch.zeros(I ** N, dtype=torch.int64, device=s.device)
+    offs = torch.tensor([I ** (N - 1 - k) for k in range(N)], device=s.device, dtype=torch.int64)
+    for _ in range(reps):
+        samples, _, _ = s.draw(N + 1)
+        counts += torch.bincount((samples * offs[:, None]).sum(0), minlength=I ** N)
+    emp = counts.cpu().numpy() / (reps * J)
+    return {"tv": float(0.5 * np.abs(emp - p).sum()),
+            "noise": float(0.5 * np.sum(np.sqrt(2 * p / (np.pi * reps * J)))),
+            "draws": reps * J, "krp_rows": I ** N}
 
 
 # ------------------------------------------------------------ our arm
@@ -261,6 +344,9 @@ def run_ours(args, ws, rank, local):
             torch.distributed.barrier()
 
     def time_draws(sampler, steps, warmup, clocks=None, jj=None):
+        """Mean ms per draw over `steps` timed draws, and the mean duration
+        of the descent launches inside that same timed region (CUDA events
+        on the launching stream)."""
         jj = j if jj is None else jj
         for _ in range(warmup):
             sampler.draw(jj)
@@ -269,6 +355,7 @@ def run_ours(args, ws, rank, local):
         if clocks:
             clocks.start()
             time.sleep(0.25)
+        sampler.descent_events = []
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(st)
@@ -278,35 +365,20 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize(dev)
         barrier()
         clk = clocks.stop() if clocks else None
+        kms = statistics.fmean(a.elapsed_time(b) for a, b in sampler.descent_events)
+        sampler.descent_events = None
         ms = max_over_ranks(e0.elapsed_time(e1) / steps, ws, dev)
-        return ms, clk
+        return ms, max_over_ranks(kms, ws, dev), clk
 
     s = ftl.Sampler(U, J, R, "efficient", precision=args.precision, seed=seeds["sampler"])
     clocks = ClockSampler(local) if rank == 0 else None
-    ms, clk = time_draws(s, args.steps, args.warmup, clocks)
+    ms, kernel_ms, clk = time_draws(s, args.steps, args.warmup, clocks)
     value = whole_job_rate(ws, J, ms / 1e3)
-
-    # descent kernel alone (roofline): computeM once, then timed launches
-    _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), j, st.cuda_stream)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    ksteps = max(20, args.steps // 3)
-    for _ in range(3):
-        _lib.call("ftl_krp_sample", ctypes.byref(s._plan), j, s.samples_dev.data_ptr(),
-                  s.h_dev.data_ptr(), s.weights_dev.data_ptr(), None, s.seed, 0, st.cuda_stream)
-    e0.record(st)
-    for i in range(ksteps):
-        _lib.call("ftl_krp_sample", ctypes.byref(s._plan), j, s.samples_dev.data_ptr(),
-                  s.h_dev.data_ptr(), s.weights_dev.data_ptr(), None, s.seed,
-                  (i + 1) * 2 * N * J, st.cuda_stream)
-    e1.record(st)
-    torch.cuda.synchronize(dev)
-    kernel_ms = e0.elapsed_time(e1) / ksteps
     prec_bytes = 4 if args.precision == "fp32" else 8
     alg = algorithmic_bytes(s.samples_dev, s.dims, R, J, N, j, prec_bytes, shadow=s.U32 is not None)
     peak, peak_kind = measured_peak()
     achieved = alg / (kernel_ms / 1e3) / 1e9
-    traffic = read_traffic(args.precision)
+    traffic, traffic_src = read_traffic(args.precision)
 
     # end to end through the public numpy API: host uniforms in (pinned),
     # samples / h / weights back into host arrays, every step
@@ -329,25 +401,54 @@ def run_ours(args, ws, rank, local):
            "api": "Sampler.KRPDrawSamples_materialize(j, samples, h_out, weights_out, draws=pinned host uniforms)"}
 
     # the other C2 variant: one mode excluded (j = 0, two descents per sample)
-    ms_j0, _ = time_draws(s, max(20, args.steps // 5), max(3, args.warmup // 4), jj=0)
-    one_excluded = {"j": 0, "value": whole_job_rate(ws, J, ms_j0 / 1e3), "ms_per_step": ms_j0}
+    ms_j0, kms_j0, _ = time_draws(s, max(20, args.steps // 5), max(3, args.warmup // 4), jj=0)
+    one_excluded = {"j": 0, "value": whole_job_rate(ws, J, ms_j0 / 1e3), "ms_per_step": ms_j0,
+                    "descent_ms": kms_j0}
 
-    # the plain FP64 GPU path on the same workload, for the mixed/FP64 ratio
+    # the plain FP64 GPU path on the same workload (the like-for-like
+    # precision of the reference), and the accuracy of the mixed path
+    # against it: both drawn with the same uniforms
     fp64 = None
+    acc = {}
+    shared = torch.empty(2 * N * J, dtype=torch.float64, device=dev)
+    shared.uniform_(0.0, 1.0, generator=torch.Generator(device=dev).manual_seed(4242))
+    smp, _, w_mixed = s.draw(j, shared)
+    samples_mixed, w_mixed = smp.clone(), w_mixed.clone()
     if args.precision == "fp32" and not args.no_fp64_arm:
+        s.descent_events = None
         del s
         torch.cuda.empty_cache()
         s64 = ftl.Sampler(U, J, R, "efficient", precision="fp64", seed=seeds["sampler"])
-        ms64, _ = time_draws(s64, max(10, args.steps // 5), max(3, args.warmup // 4))
-        fp64 = {"value": whole_job_rate(ws, J, ms64 / 1e3), "ms_per_step": ms64}
+        ms64, kms64, _ = time_draws(s64, max(10, args.steps // 5), max(3, args.warmup // 4))
+        fp64 = {"value": whole_job_rate(ws, J, ms64 / 1e3), "ms_per_step": ms64, "descent_ms": kms64}
+        smp64, _, w64 = s64.draw(j, shared)
+        same = (samples_mixed == smp64).all(dim=0)
+        mism = int((~same).sum())
+        wrel = ((w_mixed - w64).abs() / w64.abs())[same]
+        acc["mixed_vs_fp64_same_uniforms"] = {
+            "samples": J, "index_agreement": 1.0 - mism / J, "mismatches": mism,
+            "tv_upper_bound_95": binom_upper(mism, J),
+            "weights_rel_err_max": float(wrel.max()) if wrel.numel() else None,
+            "weights_rel_err_median": float(wrel.median()) if wrel.numel() else None,
+            "note": "coupling: TV(mixed law, FP64 law) <= P(indices differ under shared uniforms)"}
+        samples64_host = smp64.cpu().numpy().astype(np.uint64)
         del s64
+        torch.cuda.empty_cache()
+    else:
+        samples64_host = None
+        del s
+    if rank == 0:
+        acc["small_krp_tv"] = {p: small_krp_tv(ftl, p) for p in ("fp32", "fp64")}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         U_host = [u.cpu().numpy() for u in U]
         del U
         torch.cuda.empty_cache()
-        cpu = cpu_baseline(U_host, J, R, j, reps=3)
+        cpu, par = cpu_baseline(U_host, J, R, j, reps=3, shared=shared.cpu().numpy(),
+                                samples64=samples64_host, samples_mixed=samples_mixed.cpu().numpy())
+        if par is not None:
+            acc.update(par)
 
     if rank != 0:
         return None
@@ -357,6 +458,9 @@ def run_ours(args, ws, rank, local):
         "vs_baseline": None, "dtype": args.precision, "data": "synthetic (seeded N(0,1), 1% rows x100)",
         "config": {"workload": "exact KRP leverage sampling, N=3, I=2^23, R=32, J=50000, no mode excluded",
                    "N": N, "I": I, "R": R, "J": J, "j": j, "precision": args.precision,
+                   "value_is": ("mixed precision (FP32 node Grams and forms, FP64 h, weights, pseudo-inverse): "
+                                "the north-star mixed-precision target; fp64_path is the reference's precision")
+                   if args.precision == "fp32" else "FP64 throughout (the reference's precision)",
                    "l2": "inputs larger than L2 (partition trees 3 x %.2f GB)" % (
                        (2 * (I // R) - 1) * (R * (R + 1) // 2) * prec_bytes / 1e9),
                    "parallelism": f"replicas x{ws}"},
@@ -365,12 +469,15 @@ def run_ours(args, ws, rank, local):
         # krp_fixup_kernel (FP32; FP64 draws have no fix-up pass)
         "gpu_launches": (4 if args.precision == "fp32" else 3) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "krp_draw_kernel", "kernel_ms": kernel_ms,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_kind": peak_kind, "kernel": "krp_draw_kernel",
+                     "kernel_ms": kernel_ms, "kernel_ms_source": "mean of the descent launches in the timed loop "
+                     "(krp_draw_kernel + its fix-up pass), CUDA events on the launching stream",
                      "algorithmic_bytes_per_launch": alg},
         "clocks": clk,
         "cpu_baseline": cpu,
         "one_mode_excluded": one_excluded,
+        "accuracy": acc,
     }
     if fp64 is not None:
         line["fp64_path"] = fp64
@@ -378,10 +485,14 @@ def run_ours(args, ws, rank, local):
     return line
 
 
-def cpu_baseline(U_host, J, R, j, reps=3):
+def cpu_baseline(U_host, J, R, j, reps=3, shared=None, samples64=None, samples_mixed=None):
     """The CPU oracle port (C restatement of the reference's sampler with
     OpenMP over samples) on the same workload: full-size trees (built outside
-    the timing), one warm-up draw, median of `reps` draws of J samples."""
+    the timing), one warm-up draw, median of `reps` draws of J samples.
+    As the checker it then draws with the uniforms the GPU paths used and
+    compares indices: the FP64 GPU path must match it except at near-ties
+    (decision margin < 1e-10), and the mixed path's mismatches are binned by
+    the oracle's margin."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     O.set_threads(threads)
@@ -396,8 +507,31 @@ def cpu_baseline(U_host, J, R, j, reps=3):
         o.draw(j, draws)
         ts.append(time.perf_counter() - t0)
     t = statistics.median(ts)
-    return {"value": J / t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{reps} draws of J={J} (median) at the full workload, trees prebuilt"}
+    cpu = {"value": J / t, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{reps} draws of J={J} (median) at the full workload, trees prebuilt",
+           "note": "the port parallelises over samples with OpenMP; the reference calls cblas_dsymv once per "
+                   "sample and level, so this baseline is stronger than the reference itself"}
+    par = None
+    if shared is not None:
+        ref = o.draw(j, shared, want_margin=True).astype(np.uint64)
+        margin = o.margin
+        par = {}
+
+        def bins(bad):
+            m = margin[bad]
+            return {"margin_lt_1e-10": int((m < 1e-10).sum()), "margin_lt_1e-6": int((m < 1e-6).sum()),
+                    "margin_lt_1e-3": int((m < 1e-3).sum()), "total": int(bad.sum())}
+
+        if samples64 is not None:
+            bad = (samples64 != ref).any(axis=0)
+            par["fp64_vs_oracle"] = {"samples": J, "index_exact": float(1 - bad.mean()),
+                                     "mismatches": bins(bad),
+                                     "ok": bool(np.all(margin[bad] < 1e-10))}
+        if samples_mixed is not None:
+            bad = (samples_mixed.astype(np.uint64) != ref).any(axis=0)
+            par["mixed_vs_oracle"] = {"samples": J, "index_agreement": float(1 - bad.mean()),
+                                      "mismatches": bins(bad)}
+    return cpu, par
 
 
 # ------------------------------------------------------- reference arm
@@ -416,10 +550,9 @@ def run_reference(args, ws, rank):
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     O.set_threads(threads)
-    # each step: one draw of J_step samples (bounded so the run stays short)
-    J_step = min(J, 10000)
-    o = O.OracleKRPSampler(U, J_step, R)
-    draws = rng.random(2 * N * J_step)
+    # each step: one draw of J samples, the GPU arm's configuration
+    o = O.OracleKRPSampler(U, J, R)
+    draws = rng.random(2 * N * J)
     for _ in range(max(1, args.warmup)):
         o.draw(j, draws)
     steps = max(1, min(args.steps, 20))
@@ -427,16 +560,19 @@ def run_reference(args, ws, rank):
     for _ in range(steps):
         o.draw(j, draws)
     t = time.perf_counter() - t0
-    value = steps * J_step / t
+    value = steps * J / t
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded N(0,1), 1% rows x100)",
         "config": {"workload": "exact KRP leverage sampling, N=3, I=2^23, R=32, J=50000, no mode excluded",
-                   "N": N, "I": I, "R": R, "J": J, "j": j, "samples_per_step": J_step},
+                   "N": N, "I": I, "R": R, "J": J, "j": j, "samples_per_step": J},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} draws of {J_step} samples at the full workload"},
+                         "sample": f"{steps} draws of J={J} samples at the full workload (the GPU arm's config)",
+                         "note": "C restatement of the reference's sampler (the reference's sources are not on "
+                                 "the GPU box); it parallelises over samples with OpenMP, where the reference "
+                                 "calls cblas_dsymv per sample and level"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -638,7 +774,15 @@ def run_serve(args, ws, rank, local):
 
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this script as args.gpus ranks
+        sys.exit(subprocess.call(spawn_command(sys.argv[1:], args.gpus)))
     ws, rank, local = dist_setup()
+    if args.workload == "launcher-check":
+        line = launcher_check(ws, rank, local)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
     if args.workload == "serve":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop"}), flush=True)

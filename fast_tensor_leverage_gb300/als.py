@@ -222,7 +222,11 @@ class ALS:
         cur.wait_stream(cap)
 
     def replay_sweep(self) -> None:
-        """Run one captured sweep on the current stream."""
+        """Run one captured sweep on the current stream.  The device counter
+        is first refilled from the host one (a stream-ordered fill), so eager
+        updates made between replays advance the stream the replay draws from
+        and no uniforms are reused."""
+        self._ctr_dev.fill_(self.sampler.counter)
         self._graph.replay()
         # keep the host copy of the Philox counter in step with the device one
         N, J = self.cp_decomp.N, self.J

@@ -22,7 +22,6 @@
 
 namespace ftl {
 
-int num_sms();
 
 struct KeyRadix {
     int N, j;
@@ -1215,17 +1214,17 @@ extern "C" int ftl_weighted_gram(const double *lhs, const int32_t *rowidx, const
     const int nblk = num_sms();
     cudaStream_t st = (cudaStream_t)stream;
     const size_t smem = (size_t)(64 * R) * sizeof(double);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(gram_partial_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        cudaFuncSetAttribute(gram_partial_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        cudaFuncSetAttribute(gram_partial_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        cudaFuncSetAttribute(gram_partial_kernel<9>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        attr = true;
-    }
     const int P = packed_size(R);
     const int threads = gram_threads(R);
     const int ept = (P + threads - 1) / threads;
+    {
+        const void *fn = ept <= 1   ? (const void *)gram_partial_kernel<1>
+                         : ept <= 2 ? (const void *)gram_partial_kernel<2>
+                         : ept <= 4 ? (const void *)gram_partial_kernel<4>
+                                    : (const void *)gram_partial_kernel<9>;
+        const int arc = ensure_smem(fn, smem, "gram_partial_kernel");
+        if (arc) return arc;
+    }
     double *part = (double *)workspace;
     if (ept <= 1)
         gram_partial_kernel<1><<<nblk, threads, smem, st>>>(lhs, rowidx, w, cnt, n_rows_dev, n_rows, R, part);
@@ -1247,10 +1246,9 @@ extern "C" int ftl_pinv_square(const double *M, int R, int target_rank, const in
     const bool vglob = (size_t)(2 * R * R + R + 2) * sizeof(double) > 200 * 1024;
     FTL_CHECK_ARG(!vglob || vscratch, "ftl_pinv_square: R=%d needs an R*R FP64 scratch buffer", R);
     const size_t smem = (size_t)((vglob ? 1 : 2) * R * R + R + 2) * sizeof(double) + (2 * R + 4) * sizeof(int) + 16;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(pinv_square_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr = true;
+    {
+        const int arc = ensure_smem((const void *)pinv_square_kernel, smem, "pinv_square_kernel");
+        if (arc) return arc;
     }
     pinv_square_kernel<<<1, 512, smem, (cudaStream_t)stream>>>(M, R, target_rank, rank_cap_dev, tol, out,
                                                                 vglob ? vscratch : nullptr);
@@ -1282,12 +1280,11 @@ extern "C" int ftl_solve_rows(const double *B, const double *pinv, int64_t I, in
     // (96 KB), 64 threads above (196 KB at R = 128)
     const int threads = R > 64 ? 64 : 128;
     const size_t smem = (size_t)(R * R + threads * R) * sizeof(double);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(solve_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr = true;
-    }
     FTL_CHECK_ARG(smem <= 227 * 1024, "ftl_solve_rows: R=%d too large", R);
+    {
+        const int arc = ensure_smem((const void *)solve_rows_kernel, smem, "solve_rows_kernel");
+        if (arc) return arc;
+    }
     int blocks = (int)std::min<int64_t>((I + threads - 1) / threads, (int64_t)num_sms() * 8);
     solve_rows_kernel<<<blocks, threads, smem, (cudaStream_t)stream>>>(B, pinv, I, R, U);
     return check_launch("solve_rows_kernel");

@@ -16,7 +16,6 @@
 #include "ftl_common.cuh"
 
 namespace ftl {
-int num_sms();  // tree_build.cu
 }
 
 struct ftl_sparse {

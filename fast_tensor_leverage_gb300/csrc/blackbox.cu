@@ -24,7 +24,6 @@
 
 namespace ftl {
 
-int num_sms();
 
 struct BBFactors {
     const double *U[FTL_MAX_MODES];
@@ -397,11 +396,8 @@ static int dense_geom(DenseGeom &dg, const int64_t *dims, int N) {
 }
 
 static int smem_attr(const void *fn, size_t bytes) {
-    if (bytes > 48 * 1024) {
-        FTL_CHECK_ARG(bytes <= 227 * 1024, "shared memory request of %zu bytes", bytes);
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    }
-    return FTL_OK;
+    FTL_CHECK_ARG(bytes <= 227 * 1024, "shared memory request of %zu bytes", bytes);
+    return ensure_smem(fn, bytes, "black-box MTTKRP kernel");
 }
 
 }  // namespace ftl

@@ -282,15 +282,14 @@ int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st) 
     p.v_global = cm_smem_bytes(plan->R, false) > 200 * 1024;
     size_t smem = cm_smem_bytes(plan->R, p.v_global);
     if (smem > 227 * 1024) return fail(FTL_E_UNSUPPORTED, "computeM: R=%d too large", plan->R);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(computem_pinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        cudaFuncSetAttribute(computem_eig_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        cudaFuncSetAttribute(computem_eig_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
-    }
+    int rc = ensure_smem((const void *)computem_pinv_kernel, smem, "computem_pinv_kernel");
+    if (!rc)
+        rc = plan->prec == FTL_PREC_FP64
+                 ? ensure_smem((const void *)computem_eig_kernel<double>, smem, "computem_eig_kernel")
+                 : ensure_smem((const void *)computem_eig_kernel<float>, smem, "computem_eig_kernel");
+    if (rc) return rc;
     computem_pinv_kernel<<<1, FTL_CM_THREADS, smem, st>>>(p);
-    int rc = check_launch("computem_pinv_kernel");
+    rc = check_launch("computem_pinv_kernel");
     if (rc) return rc;
     if (plan->prec == FTL_PREC_FP64)
         computem_eig_kernel<double><<<plan->N, FTL_CM_THREADS, smem, st>>>(p);

@@ -2,6 +2,7 @@
 #include <cstdarg>
 #include <cstdio>
 
+#include "attr_registry.h"
 #include "ftl_common.cuh"
 
 namespace ftl {
@@ -27,6 +28,37 @@ int check_launch(const char *what) {
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return fail(FTL_E_CUDA, "%s: %s", what, cudaGetErrorString(err));
     return FTL_OK;
+}
+
+static AttrRegistry g_smem_attrs;
+
+int ensure_smem(const void *func, size_t bytes, const char *name) {
+    if (bytes <= 48 * 1024) return FTL_OK;
+    if (bytes > 227 * 1024) return fail(FTL_E_UNSUPPORTED, "%s: %zu bytes of shared memory requested", name, bytes);
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return fail(FTL_E_CUDA, "%s: cudaGetDevice: %s", name, cudaGetErrorString(err));
+    const int rc = g_smem_attrs.ensure(func, dev, (int)bytes, [func](int b) {
+        return (int)cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    });
+    if (rc != 0)
+        return fail(FTL_E_CUDA, "%s: raising the shared-memory limit to %zu bytes: %s", name, bytes,
+                    cudaGetErrorString((cudaError_t)rc));
+    return FTL_OK;
+}
+
+constexpr int kMaxDevices = 64;
+static int g_sm_count[kMaxDevices] = {0};
+
+int num_sms() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+    int n = __atomic_load_n(&g_sm_count[dev], __ATOMIC_RELAXED);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        __atomic_store_n(&g_sm_count[dev], n, __ATOMIC_RELAXED);
+    }
+    return n;
 }
 
 }  // namespace ftl

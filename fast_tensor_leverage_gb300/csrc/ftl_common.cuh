@@ -16,6 +16,15 @@ void set_error(const char *fmt, ...);
 int fail(int status, const char *fmt, ...);
 int check_launch(const char *what);
 
+// Raise `func`'s dynamic shared-memory limit to at least `bytes` on the
+// current device (a no-op below the 48 KB default, and once per kernel,
+// device and size); FTL_E_CUDA with `name` in the message when the runtime
+// refuses.
+int ensure_smem(const void *func, size_t bytes, const char *name);
+
+// SM count of the current device (cached per device).
+int num_sms();
+
 #define FTL_CHECK_ARG(cond, ...)                                  \
     do {                                                          \
         if (!(cond)) return ::ftl::fail(FTL_E_ARG, __VA_ARGS__);  \

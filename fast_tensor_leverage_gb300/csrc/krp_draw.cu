@@ -16,7 +16,6 @@
 namespace ftl {
 
 int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st);
-int num_sms();
 
 struct DrawParams {
     int N, R, P, S;
@@ -357,22 +356,18 @@ template <int RMAX, typename T, bool S32>
 static int launch_draw(const DrawParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(krp_draw_kernel<RMAX, T, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max<size_t>(smem, 48 * 1024));
-        attr = true;
+    {
+        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32>, smem, "krp_draw_kernel");
+        if (arc) return arc;
     }
     int64_t blocks = (p.J + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
     krp_draw_kernel<RMAX, T, S32><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     int rc = check_launch("krp_draw_kernel");
     if (rc || sizeof(T) == 8) return rc;
-    static bool fattr = false;
-    if (!fattr) {
-        cudaFuncSetAttribute(krp_fixup_kernel<RMAX, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max<size_t>(smem, 48 * 1024));
-        fattr = true;
+    {
+        const int arc = ensure_smem((const void *)krp_fixup_kernel<RMAX, S32>, smem, "krp_fixup_kernel");
+        if (arc) return arc;
     }
     int64_t fblocks = (p.J + 32 * warps - 1) / (32 * warps);
     fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
@@ -384,11 +379,9 @@ template <int RMAX, typename T, bool S32>
 static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(krp_draw_multi_kernel<RMAX, T, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max<size_t>(smem, 48 * 1024));
-        attr = true;
+    {
+        const int arc = ensure_smem((const void *)krp_draw_multi_kernel<RMAX, T, S32>, smem, "krp_draw_multi_kernel");
+        if (arc) return arc;
     }
     const int64_t total = mp.cum[mp.n];
     int64_t blocks = (total + warps - 1) / warps;
@@ -396,11 +389,9 @@ static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
     krp_draw_multi_kernel<RMAX, T, S32><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
     int rc = check_launch("krp_draw_multi_kernel");
     if (rc || sizeof(T) == 8) return rc;
-    static bool fattr = false;
-    if (!fattr) {
-        cudaFuncSetAttribute(krp_fixup_multi_kernel<RMAX, S32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max<size_t>(smem, 48 * 1024));
-        fattr = true;
+    {
+        const int arc = ensure_smem((const void *)krp_fixup_multi_kernel<RMAX, S32>, smem, "krp_fixup_multi_kernel");
+        if (arc) return arc;
     }
     int64_t fblocks = (total + 32 * warps - 1) / (32 * warps);
     fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
@@ -412,11 +403,9 @@ template <int RMAX, typename T>
 static int launch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T>();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(tree_sample_kernel<RMAX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max<size_t>(smem, 48 * 1024));
-        attr = true;
+    {
+        const int arc = ensure_smem((const void *)tree_sample_kernel<RMAX, T>, smem, "tree_sample_kernel");
+        if (arc) return arc;
     }
     int64_t blocks = (p.J + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));

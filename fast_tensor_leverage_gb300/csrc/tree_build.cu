@@ -164,12 +164,10 @@ __global__ void __launch_bounds__(256) levels_fused_kernel(V *__restrict__ G, in
     }
 }
 
-static int sm_count();
-
 template <typename V, int H>
 static void launch_fused(V *G, int64_t top_start, int64_t top_count, int S16, cudaStream_t st) {
     const int64_t total = top_count * S16;
-    const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
     levels_fused_kernel<V, H><<<std::max(blocks, 1), 256, 0, st>>>(G, top_start, top_count, S16);
 }
 
@@ -183,18 +181,6 @@ __global__ void tree_scale_kernel(const T *__restrict__ src, T *__restrict__ dst
     }
 }
 
-static int sm_count() {
-    static int cached = 0;
-    if (!cached) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
-        if (cached <= 0) cached = 148;
-    }
-    return cached;
-}
-
-int num_sms() { return sm_count(); }
 
 template <typename T>
 static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaStream_t st) {
@@ -212,22 +198,17 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     if (smem > 227 * 1024)
         return fail(FTL_E_UNSUPPORTED, "tree_build: leaf block of %lld x %d needs %zu B of shared memory",
                     (long long)F, R, smem);
-    // once per process (one device): changing a kernel's attributes on every
-    // call can wait for launches of it that are still running
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(leaf_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr = true;
-    }
+    int rc = ensure_smem((const void *)leaf_gram_kernel<T>, smem, "leaf_gram_kernel");
+    if (rc) return rc;
     int64_t nbatch = (geom.leaf_count + LB - 1) / LB;
     // one wave of resident CTAs, each looping over batches: a grid larger
     // than what fits at once leaves a partial second wave
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_gram_kernel<T>, 256, smem) != cudaSuccess || occ < 1)
         occ = 1;
-    int grid = (int)std::min<int64_t>(nbatch, (int64_t)sm_count() * occ);
+    int grid = (int)std::min<int64_t>(nbatch, (int64_t)num_sms() * occ);
     leaf_gram_kernel<T><<<grid, 256, smem, st>>>(U, n, R, RP, g, LB, G);
-    int rc = check_launch("leaf_gram_kernel");
+    rc = check_launch("leaf_gram_kernel");
     if (rc) return rc;
     using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
     const int S16 = node_stride(R, sizeof(T)) * (int)sizeof(T) / 16;
@@ -236,7 +217,7 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     const int64_t end = geom.node_count - geom.leaf_count;
     if (end > start) {
         const int64_t total = (end - start) * (int64_t)S16;
-        const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+        const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
         if (total < (int64_t)INT32_MAX)
             level_sum_kernel<V, uint32_t><<<blocks, 256, 0, st>>>((V *)G, start, end, S16);
         else
@@ -319,7 +300,7 @@ extern "C" int ftl_tree_scale(const void *G_src, void *G_dst, int64_t node_count
     const int P = packed_size(R);
     const int S = node_stride(R, prec == FTL_PREC_FP64 ? 8 : 4);
     int64_t total = node_count * (int64_t)S;
-    int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
+    int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
     cudaStream_t st = (cudaStream_t)stream;
     if (prec == FTL_PREC_FP64)
         tree_scale_kernel<double><<<blocks, 256, 0, st>>>((const double *)G_src, (double *)G_dst, total, P, S, mat);

@@ -94,6 +94,9 @@ class Sampler:
         self._spec = None
         self._last_j = None
         self._tree_ev = torch.cuda.Event()
+        # optional list: each draw appends a (start, end) pair of timing
+        # events recorded on the launching stream around its descent launch
+        self.descent_events = None
         self._refresh_plan()
         for k in range(N):
             self.update_sampler(k)
@@ -189,9 +192,11 @@ class Sampler:
             d_ptr = dt.data_ptr()
         if self._overlap:
             main.wait_event(self._cm_done[b])
+            ev0 = self._timing_event(main)
             _lib.call("ftl_krp_sample", ctypes.byref(plan), j, self.samples_dev.data_ptr(),
                       self.h_dev.data_ptr(), self.weights_dev.data_ptr(), d_ptr, self.seed,
                       self.counter, int(main.cuda_stream))
+            self._timing_event(main, ev0)
             ev = torch.cuda.Event()
             ev.record(main)
             self._set_free[b] = ev
@@ -209,6 +214,17 @@ class Sampler:
         if d_ptr is None:
             self.counter += 2 * self.N * self.J
         return self.samples_dev, self.h_dev, self.weights_dev
+
+    def _timing_event(self, stream, start=None):
+        # records a timing event on `stream` when descent_events is a list;
+        # with `start`, appends the (start, end) pair
+        if self.descent_events is None:
+            return None
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        if start is not None:
+            self.descent_events.append((start, ev))
+        return ev
 
     def _launch_computem(self, b: int, j: int) -> None:
         # computeM into workspace set b after the trees it reads and after the

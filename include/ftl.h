@@ -440,7 +440,10 @@ int ftl_gram_hadamard(const double *const *grams_dev, int N, int R, int exclude,
  * first call on a device looks up the array's address with that device
  * current; make it before any stream capture.  All calls share the array
  * (each clears the part it uses): calls that overlap on the GPU race and
- * must be serialised by the caller.  Allocates nothing. */
+ * must be serialised by the caller.  FP32 draws here read their leaf blocks
+ * from the FP64 factors (there is no argument for FP32 factor copies), with
+ * the same results as ftl_krp_draw and a slower leaf scan.  Allocates
+ * nothing. */
 int ftl_krp_draw_static(int N, int R, int64_t J, int prec, const int64_t *dims,
                         const double *const *U_dev, void *const *gram_G_dev, uint32_t j,
                         uint64_t *samples_dev, double *h_dev, double *weights_dev,

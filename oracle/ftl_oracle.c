@@ -9,7 +9,7 @@
  * of a full R x R buffer whose lower triangle is left zero.  Arithmetic and
  * every decision follow the reference line by line (cited per function).
  * Its own results are pinned against the reference module built from the
- * reference sources (oracle/Makefile) by tests/test_oracle_pinning.py and
+ * reference sources (oracle/Makefile) by tests/test_oracle.py and
  * the committed fixtures in tests/golden/.
  */
 #include <math.h>

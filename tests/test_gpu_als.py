@@ -160,6 +160,38 @@ def test_gpu_als_fp32_rank64_four_modes_stays_finite(ftl):
     assert np.isfinite(resid)
 
 
+def test_replay_after_eager_update_draws_fresh_uniforms(ftl):
+    """An eager sampled update between two replays of a captured sweep
+    advances the Philox stream the next replay draws from: the replay's last
+    mode uses the uniforms at host counter + (N-1) 2NJ, none that the eager
+    update already used."""
+    from fast_tensor_leverage_gb300 import _lib
+    from fast_tensor_leverage_gb300.synthetic import sparse_powerlaw_tensor
+    dims, J, R = [3000, 2500, 2000], 512, 8
+    N = len(dims)
+    idx, vals = sparse_powerlaw_tensor(dims, 40000, 1.1, seed=5, device="cuda")
+    sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
+    rng = np.random.default_rng(8)
+    lr = ftl.LowRankTensor(R, [rng.normal(size=(d, R)) for d in dims], sync_host=False)
+    lr.renormalize_columns(-1)
+    als = ftl.ALS(lr, sp)
+    als.initialize_ds_als(J, "efficient", precision="fp64", seed=6)
+    for j in range(N):
+        als.execute_ds_als_update(j, True, True)
+    als.capture_sweep()
+    als.replay_sweep()
+    als.execute_ds_als_update(0, True, True)
+    c = als.sampler.counter
+    als.replay_sweep()
+    torch.cuda.synchronize()
+    expect = torch.empty(2 * N * J, dtype=torch.float64, device="cuda")
+    _lib.call("ftl_philox_uniforms", expect.data_ptr(), 2 * N * J, als.sampler.seed, c + (N - 1) * 2 * N * J,
+              torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert torch.equal(als._gdraws.reshape(-1), expect)
+    assert als.sampler.counter == c + N * 2 * N * J
+
+
 def test_gpu_exact_als_update_rank128_matches_numpy(ftl):
     """Exact update at the largest rank (R = 128: the solve stages 64 rows
     per block, the pseudo-inverse keeps its eigenvectors in global scratch)

@@ -58,3 +58,23 @@ def test_bench_multirank_host_logic_gloo():
     assert res[0]["seeds"]["sampler"] != res[1]["seeds"]["sampler"]
     assert not res[0]["ref_is_none"] and res[0]["ref_impl"] == "reference"
     assert res[1]["ref_is_none"]                           # rank 1 runs no reference work
+
+
+def test_bench_spawns_its_own_ranks():
+    """`bench.py --gpus 2` without an external launcher relaunches itself as
+    two ranks (torch.distributed.run on 127.0.0.1); the ranks rendezvous,
+    take the max over ranks and only rank 0 prints its line."""
+    import json
+    import subprocess
+    env = dict(os.environ)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    res = subprocess.run([sys.executable, str(REPO / "bench.py"), "--gpus", "2", "--workload", "launcher-check"],
+                         capture_output=True, text=True, timeout=240, env=env, cwd=str(REPO))
+    assert res.returncode == 0, res.stderr[-2000:]
+    lines = [json.loads(ln) for ln in res.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, res.stdout
+    line = lines[0]
+    assert line["n_gpus"] == 2 and line["rank"] == 0 and line["local_rank"] == 0
+    assert line["max_over_ranks"] == 2.0                   # rank 1's value
+    assert line["whole_job_rate"] == 2 * 100.0 / 2.0
