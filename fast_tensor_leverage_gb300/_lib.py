@@ -22,7 +22,14 @@ STATUS_NAMES = {
     5: "FTL_E_CANCELLED",
     6: "FTL_E_UNSUPPORTED",
 }
-PREC = {"fp64": 0, "fp32": 1}
+# tree precisions: fp64 and fp32 trees computed in their precision; tf32x3
+# and bf16 trees store FP32 nodes whose leaf Grams come from the tensor cores
+PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16": 3}
+
+
+def storage_prec(prec: int) -> int:
+    """The node precision plans and draws see (FP64 or FP32)."""
+    return 0 if prec == 0 else 1
 MAX_MODES = 16
 MAX_RANK = 128
 
@@ -108,7 +115,10 @@ SIGNATURES = {
     "ftl_factor_shadow": ([_P, _I64, _P, _P], _INT),
     "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),
     "ftl_tree_bytes": ([_I64, _I64, _INT, _INT, _SZP], _INT),
+    "ftl_node_layout": ([_INT, _INT, ctypes.POINTER(_INT), ctypes.POINTER(_INT), _P], _INT),
     "ftl_tree_build": ([_P, _I64, _INT, _I64, _INT, _P, _P], _INT),
+    "ftl_tree_build_ex": ([_P, _I64, _INT, _I64, _INT, _P, _P, _P], _INT),
+    "ftl_device_status": ([ctypes.POINTER(ctypes.c_uint32)], _INT),
     "ftl_tree_scale": ([_P, _P, _I64, _INT, _INT, _P, _P], _INT),
     "ftl_tree_sample": ([_P, _INT, _P, _I64, _INT, _I64, _P, _P, _P, _P, _I64, _P], _INT),
     "ftl_krp_plan_sizes": ([_INT, _INT, _INT, _SZP, _SZP, _SZP, _SZP], _INT),
@@ -178,6 +188,26 @@ def tree_bytes(n: int, F: int, R: int, prec: int) -> int:
     out = ctypes.c_size_t()
     call("ftl_tree_bytes", n, F, R, prec, ctypes.byref(out))
     return out.value
+
+
+def node_layout(R: int, prec: int):
+    """(layout, stride, pos): the node layout id (0 packed, 1 wrapped
+    diagonals), values per node, and the position inside a node of every
+    upper-triangle element in row-major order (a numpy int32 array of
+    R(R+1)/2 entries)."""
+    import numpy as np
+    lay, stride = _INT(), _INT()
+    pos = np.zeros(R * (R + 1) // 2, dtype=np.int32)
+    call("ftl_node_layout", R, prec, ctypes.byref(lay), ctypes.byref(stride), pos.ctypes.data)
+    return lay.value, stride.value, pos
+
+
+def device_status() -> int:
+    """Status bits of device-side bounded waits that ran out since the last
+    call (waits for the device; cleared on read)."""
+    v = ctypes.c_uint32()
+    call("ftl_device_status", ctypes.byref(v))
+    return v.value
 
 
 def ws_bytes(name: str, *args) -> int:

@@ -222,7 +222,7 @@ extern "C" int ftl_als_create(const ftl_sparse *X, int R, int64_t J, int prec, u
     *out = nullptr;
     FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK && J >= 1 && J <= INT32_MAX / 4, "ftl_als_create: R=%d J=%lld", R,
                   (long long)J);
-    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_als_create: bad precision %d", prec);
+    FTL_CHECK_ARG(ftl::valid_prec(prec), "ftl_als_create: bad precision %d", prec);
     ftl_als *A = new ftl_als();
     A->X = X;
     A->N = X->N;

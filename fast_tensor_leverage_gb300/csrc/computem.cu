@@ -21,6 +21,12 @@
 
 #include "eig.cuh"
 
+// Mixed precision runs the per-mode eigensolvers in FP32 (1: in FP64, the
+// reference's precision; an accuracy diagnostic, slower on GB300's FP64 pipe).
+#ifndef FTL_CM_MIXED_EIG_FP64
+#define FTL_CM_MIXED_EIG_FP64 0
+#endif
+
 namespace ftl {
 
 struct CMParams {
@@ -35,9 +41,10 @@ struct CMParams {
     DGeom eig;                // geometry of an eigen tree (n = R, F = 1)
 };
 
-__device__ __forceinline__ double root_at(const CMParams &p, int k, int e) {
-    if (p.prec == FTL_PREC_FP64) return ((const double *)p.root[k])[e];
-    return (double)((const float *)p.root[k])[e];
+// Element (a, b) of mode k's root Gram, in the tree's layout and precision.
+__device__ __forceinline__ double root_ab(const CMParams &p, int k, int a, int b) {
+    if (p.prec == FTL_PREC_FP64) return ((const double *)p.root[k])[node_pos(a, b, p.R, 8)];
+    return (double)((const float *)p.root[k])[node_pos(a, b, p.R, 4)];
 }
 
 // Shared memory: A (R*R), V (R*R unless kept in global scratch), cs (R+2),
@@ -63,8 +70,7 @@ __global__ void computem_pinv_kernel(CMParams p) {
         if ((uint32_t)k == p.j) continue;
         for (int e = tid; e < RR; e += nth) {
             int a = e / R, b = e - a * R;
-            int lo = min(a, b), hi = max(a, b);
-            double g = root_at(p, k, packed_index(lo, hi, R));
+            double g = root_ab(p, k, a, b);
             double prev = (last == N) ? 1.0 : p.M[(size_t)last * RR + e];
             p.M[(size_t)k * RR + e] = g * prev;
         }
@@ -77,7 +83,7 @@ __global__ void computem_pinv_kernel(CMParams p) {
     }
     double *status = p.M + cm_status_offset(N, R);  // 1.0: Cholesky path taken
     bool chol = false;
-    if (p.prec == FTL_PREC_FP32) {
+    if (p.prec == FTL_PREC_FP32 && !FTL_CM_MIXED_EIG_FP64) {
         // Mixed mode: when every eigenvalue of M[0] exceeds the reference's
         // 1e-8 cut, its pseudo-inverse is the inverse, computed in FP64 from
         // the Cholesky factor: pinv = L^-T L^-1.  The cut is certified by
@@ -152,15 +158,31 @@ __global__ void computem_pinv_kernel(CMParams p) {
     for (int e = tid; e < RR; e += nth) {
         p.M[e] = A[e];
         int a = e / R, b = e - a * R;
-        if (a <= b) {
-            int pe = packed_index(a, b, R);
-            pinv_packed[pe] = A[e];
-            p.pinv32[pe] = (float)A[e];
+        if (a <= b) pinv_packed[packed_index(a, b, R)] = A[e];
+    }
+    // zero padding up to the node stride, read by the vectorised forms
+    for (int e = p.P + tid; e < node_stride(R, 8); e += nth) pinv_packed[e] = 0.0;
+    // FP32 copy in the FP32 node layout (the weights of FP32 draws)
+    if (node_layout(R, 4) == FTL_LAYOUT_DIAG32) {
+        for (int e = tid; e < kDiag32Stride; e += nth) {
+            int a, b;
+            diag32_entry(e, a, b);
+            p.pinv32[e] = (a < R && b < R) ? (float)A[a * R + b] : 0.0f;
+        }
+    } else {
+        for (int e = tid; e < node_stride(R, 4); e += nth) {
+            float v = 0.0f;
+            if (e < p.P) {
+                int a = 0, rem = e;
+                while (rem >= R - a) {
+                    rem -= R - a;
+                    ++a;
+                }
+                v = (float)A[a * R + a + rem];
+            }
+            p.pinv32[e] = v;
         }
     }
-    // zero padding up to the node strides, read by the vectorised forms
-    for (int e = p.P + tid; e < node_stride(R, 8); e += nth) pinv_packed[e] = 0.0;
-    for (int e = p.P + tid; e < node_stride(R, 4); e += nth) p.pinv32[e] = 0.0f;
     // M[k] o= pinv for k = N-1 .. 1, k != j
     for (int k = N - 1; k >= 1; --k) {
         if ((uint32_t)k == p.j) continue;
@@ -183,7 +205,7 @@ __global__ void computem_eig_kernel(CMParams p) {
     const int offset = ((uint32_t)(k + 1) == p.j) ? k + 2 : k + 1;
     double *W = p.M + (size_t)offset * RR;
     const bool chol = p.M[cm_status_offset(N, R)] == 1.0;
-    if (p.prec == FTL_PREC_FP32 && (offset < N || chol)) {
+    if (p.prec == FTL_PREC_FP32 && !FTL_CM_MIXED_EIG_FP64 && (offset < N || chol)) {
         // Mixed mode: FP32 Jacobi of M[offset] (offset < N), or of the FP64
         // pseudo-inverse when it came from the Cholesky path (offset == N;
         // its eigenvectors are those of M[0], its eigenvalues 1/lambda, so
@@ -230,17 +252,27 @@ __global__ void computem_eig_kernel(CMParams p) {
     const DGeom g = p.eig;
     // (an eigen tree has 2R - 1 <= 255 nodes of S <= 8256 values: 32-bit indexing)
     const int leaf_count = R;
-    // leaves: one work item per (leaf u, packed row a), the row's entries
-    // b = a..R-1 contiguous in the packed layout; then the node padding
-    for (int w = tid; w < leaf_count * R; w += nth) {
-        const int u = w / R, a = w - u * R;
-        T *row = G + (int)leaf_node(g, u) * S + packed_row_offset(a, R);
-        const T wa = (T)W[u * R + a];
-        for (int b = a; b < R; ++b) row[b - a] = wa * (T)W[u * R + b];
-    }
-    for (int w = tid; w < leaf_count * (S - P); w += nth) {
-        const int u = w / (S - P);
-        G[(int)leaf_node(g, u) * S + P + (w - u * (S - P))] = T(0);
+    if (node_layout(R, sizeof(T)) == FTL_LAYOUT_DIAG32) {
+        // leaves: one work item per (leaf u, node position e)
+        for (int w = tid; w < leaf_count * S; w += nth) {
+            const int u = w / S, e = w - u * S;
+            int a, b;
+            diag32_entry(e, a, b);
+            G[(int)leaf_node(g, u) * S + e] = (a < R && b < R) ? (T)W[u * R + a] * (T)W[u * R + b] : T(0);
+        }
+    } else {
+        // leaves: one work item per (leaf u, packed row a), the row's entries
+        // b = a..R-1 contiguous in the packed layout; then the node padding
+        for (int w = tid; w < leaf_count * R; w += nth) {
+            const int u = w / R, a = w - u * R;
+            T *row = G + (int)leaf_node(g, u) * S + packed_row_offset(a, R);
+            const T wa = (T)W[u * R + a];
+            for (int b = a; b < R; ++b) row[b - a] = wa * (T)W[u * R + b];
+        }
+        for (int w = tid; w < leaf_count * (S - P); w += nth) {
+            const int u = w / (S - P);
+            G[(int)leaf_node(g, u) * S + P + (w - u * (S - P))] = T(0);
+        }
     }
     __syncthreads();
     int start = (int)(g.nodes_upto_lfill - ((g.nodes_upto_lfill + 1) / 2));  // nodes_before_lfill
@@ -256,10 +288,10 @@ __global__ void computem_eig_kernel(CMParams p) {
         end = start;
         start = (start + 1) / 2 - 1;
     }
-    for (int e = tid; e < (2 * R - 1) * S; e += nth) {
-        const int pe = e % S;
-        if (pe < P) G[e] = G[e] * (T)root_at(p, k, pe);
-    }
+    // o root, position by position (the root Gram is stored in the same
+    // layout and precision; padding is zero in both)
+    const T *root = (const T *)p.root[k];
+    for (int e = tid; e < (2 * R - 1) * S; e += nth) G[e] = G[e] * root[e % S];
 }
 
 #ifndef FTL_CM_THREADS

@@ -50,6 +50,9 @@
 #ifndef FTL_DESC_RESIDENT_F64
 #define FTL_DESC_RESIDENT_F64 512
 #endif
+#ifndef FTL_DESC_RESIDENT_D32
+#define FTL_DESC_RESIDENT_D32 768  // FP32 DIAG32 kernels: 17 outer-product weights in registers (80 registers, no spills)
+#endif
 
 namespace ftl {
 
@@ -107,9 +110,9 @@ struct NodeShape {
 
 // Per-warp shared-memory slot: the query in FP64 and in the compute type,
 // plus the packed outer product when it does not fit in registers.
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool DIAG = false>
 struct WarpSlot {
-    static constexpr size_t xx_elems = Shape<RMAX>::XX_SMEM ? NodeShape<RMAX, T>::SMAX : 0;
+    static constexpr size_t xx_elems = (Shape<RMAX>::XX_SMEM && !DIAG) ? NodeShape<RMAX, T>::SMAX : 0;
     static constexpr size_t bytes =
         ((RMAX * sizeof(double) + RMAX * sizeof(T) + xx_elems * sizeof(T)) + 15) / 16 * 16;
 };
@@ -240,6 +243,76 @@ struct QForm {
     }
 };
 
+// x^T G x against DIAG32 nodes (FP32, 16 < R <= 32; layout in
+// ftl_common.cuh): lane a keeps the 17 weights c_d x_a x_{(a+d) mod 32} of
+// its node row in registers, so a level costs four 128-bit loads and one
+// 32-bit load per lane (each a contiguous 512- or 128-byte warp access), 17
+// FMAs and one warp reduction, with no shared-memory traffic.  The query x
+// comes zero padded to 32 entries (entries R..31 zero).
+struct QFormD32 {
+    float xx[17];
+    float *s;  // unused (interface of QForm)
+    int P, S;
+
+    __device__ __forceinline__ void setup(const float *x, const uint16_t *, int lane) {
+        const float xa = x[lane];
+        xx[0] = xa * xa;
+#pragma unroll
+        for (int d = 1; d < 16; ++d) xx[d] = (xa + xa) * __shfl_sync(0xffffffffu, xa, (lane + d) & 31);
+        xx[16] = xa * __shfl_sync(0xffffffffu, xa, (lane + 16) & 31);
+    }
+
+    __device__ __forceinline__ float partial(const float *__restrict__ node, int lane) const {
+        const float4 *v = reinterpret_cast<const float4 *>(node);
+        const float4 g0 = __ldg(v + lane), g1 = __ldg(v + 32 + lane), g2 = __ldg(v + 64 + lane),
+                     g3 = __ldg(v + 96 + lane);
+        const float g16 = __ldg(node + 512 + lane);
+        float acc = g0.x * xx[0];
+        acc = fmaf(g0.y, xx[1], acc);
+        acc = fmaf(g0.z, xx[2], acc);
+        acc = fmaf(g0.w, xx[3], acc);
+        acc = fmaf(g1.x, xx[4], acc);
+        acc = fmaf(g1.y, xx[5], acc);
+        acc = fmaf(g1.z, xx[6], acc);
+        acc = fmaf(g1.w, xx[7], acc);
+        acc = fmaf(g2.x, xx[8], acc);
+        acc = fmaf(g2.y, xx[9], acc);
+        acc = fmaf(g2.z, xx[10], acc);
+        acc = fmaf(g2.w, xx[11], acc);
+        acc = fmaf(g3.x, xx[12], acc);
+        acc = fmaf(g3.y, xx[13], acc);
+        acc = fmaf(g3.z, xx[14], acc);
+        acc = fmaf(g3.w, xx[15], acc);
+        return fmaf(g16, xx[16], acc);
+    }
+
+    __device__ __forceinline__ float eval(const float *__restrict__ node, int lane) const {
+        return warp_sum(partial(node, lane));
+    }
+
+    __device__ __forceinline__ void eval2(const float *__restrict__ na, const float *__restrict__ nb, int lane,
+                                          float &ra, float &rb) const {
+        float a = partial(na, lane), b = partial(nb, lane);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        ra = a;
+        rb = b;
+    }
+};
+
+// The form type of a (rank bound, precision, layout).
+template <int RMAX, typename T, bool DIAG>
+struct QSel {
+    using type = QForm<RMAX, T>;
+};
+template <>
+struct QSel<32, float, true> {
+    using type = QFormD32;
+};
+
 // L2 prefetch of the 128-byte lines covering [p, p + bytes), one line per
 // lane per pass.  Every address issued is the start of a line that holds at
 // least one byte of the range, so it lies inside the range's allocation.
@@ -350,9 +423,9 @@ __device__ __forceinline__ void df_sub(float &th, float &tl, float m) {
     th = nh;
 }
 
-template <int RMAX>
+template <int RMAX, class QF>
 __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, const DGeom &g,
-                                           double draw, const QForm<RMAX, float> &qf, int lane,
+                                           double draw, const QF &qf, int lane,
                                            float &frac, const double *U = nullptr, int R = 0,
                                            float *mroot = nullptr) {
     int64_t c = 0;
@@ -411,9 +484,9 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
 // children at every level, never enters a child with a non-positive form
 // while its sibling's is positive, and rescales t onto the evaluated child
 // masses (t in FP64).  In exact arithmetic it samples the same distribution.
-template <int RMAX>
+template <int RMAX, class QF>
 __device__ __forceinline__ int64_t descend_careful(const float *__restrict__ G, int S, const DGeom &g,
-                                                   double draw, const QForm<RMAX, float> &qf, int lane,
+                                                   double draw, const QF &qf, int lane,
                                                    float &frac) {
     int64_t c = 0;
     if (is_leaf(g, 0)) {
@@ -666,7 +739,7 @@ __device__ __forceinline__ double stage_query(const double (&v)[Shape<RMAX>::XPL
 #pragma unroll
         for (int q = 0; q < XPL; ++q) {
             int col = lane + 32 * q;
-            if (col < R) xT[col] = (T)(v[q] * scale);
+            xT[col] = col < R ? (T)(v[q] * scale) : T(0);  // zero padded to RMAX
         }
     }
     __syncwarp();

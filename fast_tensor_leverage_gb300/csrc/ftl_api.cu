@@ -65,4 +65,4 @@ int num_sms() {
 
 extern "C" const char *ftl_last_error(void) { return ftl::g_last_error; }
 
-extern "C" int ftl_abi_version(void) { return 3; }
+extern "C" int ftl_abi_version(void) { return 4; }

@@ -96,14 +96,58 @@ __host__ __device__ inline int64_t leaf_node(const DGeom &g, int64_t leaf) {
 // ------------------------------------------------------ packed triangles
 
 __host__ __device__ inline int packed_size(int R) { return R * (R + 1) / 2; }
-// Node stride in elements: the packed triangle padded (with zeros) to a
-// multiple of 16 bytes, so every node starts 16-byte aligned and is read
+__host__ __device__ inline int packed_row_offset(int a, int R) { return a * R - a * (a - 1) / 2; }
+
+// Node layouts.
+//   PACKED: the upper triangle in row-major order, element (a,b), a <= b, at
+//     a*R - a*(a-1)/2 + b - a, zero padded to a multiple of 16 bytes.
+//   DIAG32 (FP32 nodes with 16 < R <= 32): the Gram zero padded to 32 x 32
+//     and stored by wrapped diagonals, so that lane a of a warp reads row a:
+//     G[a][(a+d) mod 32] for d = 0..15 at ((d/4)*32 + a)*4 + d%4 (four
+//     128-bit vectors per lane, each warp load 512 contiguous bytes), and
+//     G[a][(a+16) mod 32] at 512 + a.  The distance-16 entries are stored
+//     twice (once from each end); 544 values per node.
+// x^T G x over a DIAG32 node is sum_a sum_d c_d x_a x_{(a+d) mod 32} G_pos(a,d)
+// with c_0 = 1, c_1..15 = 2 and c_16 = 1 (each stored copy counted once).
+// (FTL_LAYOUT_PACKED and FTL_LAYOUT_DIAG32 are defined in ftl.h)
+constexpr int kDiag32Stride = 544;
+
+__host__ __device__ inline int node_layout(int R, int elem_bytes) {
+    return (elem_bytes == 4 && R > 16 && R <= 32) ? FTL_LAYOUT_DIAG32 : FTL_LAYOUT_PACKED;
+}
+
+// Node stride in elements: every node starts 16-byte aligned and is read
 // with 128-bit loads.
 __host__ __device__ inline int node_stride(int R, int elem_bytes) {
+    if (node_layout(R, elem_bytes) == FTL_LAYOUT_DIAG32) return kDiag32Stride;
     const int w = 16 / elem_bytes;
     return (packed_size(R) + w - 1) / w * w;
 }
-__host__ __device__ inline int packed_row_offset(int a, int R) { return a * R - a * (a - 1) / 2; }
+
+// Position of element (a, b) (either order) of a DIAG32 node; for d = 16
+// the copy stored from row a.
+__host__ __device__ inline int diag32_pos(int a, int b) {
+    int d = (b - a) & 31;
+    if (d > 16) {
+        const int t = a;
+        a = b;
+        b = t;
+        d = 32 - d;
+    }
+    return d < 16 ? (((d >> 2) * 32 + a) << 2) + (d & 3) : 512 + a;
+}
+
+// Element (a, b) stored at position e of a DIAG32 node (e < 544).
+__host__ __device__ inline void diag32_entry(int e, int &a, int &b) {
+    if (e < 512) {
+        const int d = ((e >> 7) << 2) + (e & 3);
+        a = (e >> 2) & 31;
+        b = (a + d) & 31;
+    } else {
+        a = e - 512;
+        b = (a + 16) & 31;
+    }
+}
 
 // computeM workspace layout (doubles): 2N+3 dense R x R slots, one status
 // word, then the packed FP64 pseudo-inverse at a 16-byte aligned offset
@@ -114,6 +158,39 @@ __host__ __device__ inline size_t cm_pinv64_offset(int N, int R) {
 }
 __host__ __device__ inline int packed_index(int a, int b, int R) {
     return packed_row_offset(a, R) + (b - a);
+}
+// Position of element (a, b) (either order) in a node of the layout that
+// R and the element size select.
+__host__ __device__ inline int node_pos(int a, int b, int R, int elem_bytes) {
+    if (node_layout(R, elem_bytes) == FTL_LAYOUT_DIAG32) return diag32_pos(a, b);
+    return a <= b ? packed_index(a, b, R) : packed_index(b, a, R);
+}
+
+// ------------------------------------------------------------ precisions
+
+// Tree precisions: FP64 stores FP64 nodes; FP32, TF32X3 and BF16 store FP32
+// nodes (TF32X3 and BF16 name how the leaf Grams are formed).
+inline bool valid_prec(int prec) { return prec >= FTL_PREC_FP64 && prec <= FTL_PREC_BF16; }
+inline int storage_prec(int prec) { return prec == FTL_PREC_FP64 ? FTL_PREC_FP64 : FTL_PREC_FP32; }
+inline int prec_bytes(int prec) { return prec == FTL_PREC_FP64 ? 8 : 4; }
+
+// FP64 -> FP32, round to nearest even, by integer operations for results in
+// the normal FP32 range (FP64 exponents 897..1150); zeros and FP64
+// subnormals give signed zero; the rest (FP32 subnormal results, overflow,
+// infinities, NaN) take the hardware conversion.  Same results as
+// __double2float_rn; avoids GB300's narrow FP64 pipe for the common case.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    if (e >= 897 && e <= 1150) {
+        unsigned r = ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned rest = lo & 0x1fffffffu;
+        r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float((hi & 0x80000000u) | r);
+    }
+    if (e == 0) return __uint_as_float(hi & 0x80000000u);
+    return __double2float_rn(x);
 }
 
 // ------------------------------------------------------------------ warps

@@ -43,23 +43,24 @@ __device__ __forceinline__ double get_draw(const DrawParams &p, int64_t idx) {
 
 // Per-warp state of the draw kernels: the block's pair table and the warp's
 // shared-memory slot.
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool DIAG = false>
 struct DrawWarp {
     const uint16_t *pairs;
     double *xd;
     T *xT;
-    QForm<RMAX, T> qf;
+    typename QSel<RMAX, T, DIAG>::type qf;
     int lane;
 };
 
-template <int RMAX, typename T>
-__device__ __forceinline__ void setup_draw_warp(DrawWarp<RMAX, T> &dw, unsigned char *smem_raw, int R, int P, int S) {
+template <int RMAX, typename T, bool DIAG>
+__device__ __forceinline__ void setup_draw_warp(DrawWarp<RMAX, T, DIAG> &dw, unsigned char *smem_raw, int R, int P,
+                                                int S) {
     uint16_t *pairs = (uint16_t *)smem_raw;
     build_pairs(pairs, R);
     __syncthreads();
     const int warp = threadIdx.x >> 5;
     unsigned char *slot = smem_raw + ((NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16) +
-                          warp * WarpSlot<RMAX, T>::bytes;
+                          warp * WarpSlot<RMAX, T, DIAG>::bytes;
     dw.pairs = pairs;
     dw.xd = (double *)slot;
     dw.xT = sizeof(T) == 8 ? (T *)dw.xd : (T *)(dw.xd + RMAX);
@@ -80,8 +81,8 @@ constexpr uint64_t kRedoSample = ~0ull;
 // Sample i of one draw: for every included mode the eigen-component descent
 // and the Gram-tree descent, then the weight and the row of h.  CAREFUL (FP32
 // fix-up pass only): both descents evaluate both children at every level.
-template <int RMAX, typename T, bool CAREFUL = false, bool S32 = false>
-__device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, DrawWarp<RMAX, T> &dw) {
+template <int RMAX, typename T, bool CAREFUL = false, bool S32 = false, bool DIAG = false>
+__device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, DrawWarp<RMAX, T, DIAG> &dw) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     const int R = p.R;
@@ -89,7 +90,7 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
     const uint16_t *pairs = dw.pairs;
     double *xd = dw.xd;
     T *xT = dw.xT;
-    QForm<RMAX, T> &qf = dw.qf;
+    auto &qf = dw.qf;
     const size_t RR = (size_t)R * R;
     const size_t eig_stride = (size_t)(2 * R - 1) * p.S;
     const float RJ = (float)((double)R / (double)p.J);
@@ -175,15 +176,22 @@ __device__ __forceinline__ void draw_sample(const DrawParams &p, int64_t i, Draw
     __syncwarp();
 }
 
-template <int RMAX, typename T, bool S32>
-__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Blk<RMAX, T>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
+// Threads per SM the register budget of a draw kernel is set for.
+template <typename T, bool DIAG>
+struct Resident {
+    static constexpr int value =
+        sizeof(T) == 8 ? FTL_DESC_RESIDENT_F64 : (DIAG ? FTL_DESC_RESIDENT_D32 : FTL_DESC_RESIDENT_F32);
+};
+
+template <int RMAX, typename T, bool S32, bool DIAG>
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    DrawWarp<RMAX, T> dw;
-    setup_draw_warp<RMAX, T>(dw, smem_raw, p.R, p.P, p.S);
+    DrawWarp<RMAX, T, DIAG> dw;
+    setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, p.R, p.P, p.S);
     const int warp = threadIdx.x >> 5;
     for (int64_t i = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; i < p.J;
          i += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS)
-        draw_sample<RMAX, T, false, S32>(p, i, dw);
+        draw_sample<RMAX, T, false, S32, DIAG>(p, i, dw);
 }
 
 // Packed draw: the samples of up to FTL_MAX_PACK requests of the same rank
@@ -196,18 +204,18 @@ struct MultiDrawParams {
     DrawParams req[FTL_MAX_PACK];
 };
 
-template <int RMAX, typename T, bool S32>
-__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Blk<RMAX, T>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
+template <int RMAX, typename T, bool S32, bool DIAG>
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    DrawWarp<RMAX, T> dw;
-    setup_draw_warp<RMAX, T>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+    DrawWarp<RMAX, T, DIAG> dw;
+    setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
     const int warp = threadIdx.x >> 5;
     const int64_t total = mp.cum[mp.n];
     for (int64_t g = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; g < total;
          g += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS) {
         int r = 0;
         while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
-        draw_sample<RMAX, T, false, S32>(mp.req[r], g - mp.cum[r], dw);
+        draw_sample<RMAX, T, false, S32, DIAG>(mp.req[r], g - mp.cum[r], dw);
     }
 }
 
@@ -225,11 +233,11 @@ __device__ __forceinline__ bool needs_redo(const DrawParams &p, int64_t i) {
     return bad;
 }
 
-template <int RMAX, bool S32>
+template <int RMAX, bool S32, bool DIAG>
 __global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_kernel(DrawParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    DrawWarp<RMAX, float> dw;
-    setup_draw_warp<RMAX, float>(dw, smem_raw, p.R, p.P, p.S);
+    DrawWarp<RMAX, float, DIAG> dw;
+    setup_draw_warp<RMAX, float, DIAG>(dw, smem_raw, p.R, p.P, p.S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * Blk<RMAX, float>::WARPS;
     for (int64_t b = ((int64_t)blockIdx.x * Blk<RMAX, float>::WARPS + warp) * 32; b < p.J; b += nw * 32) {
@@ -237,16 +245,16 @@ __global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_kernel
         while (bal) {
             const int src = __ffs(bal) - 1;
             bal &= bal - 1;
-            draw_sample<RMAX, float, true, S32>(p, b + src, dw);
+            draw_sample<RMAX, float, true, S32, DIAG>(p, b + src, dw);
         }
     }
 }
 
-template <int RMAX, bool S32>
+template <int RMAX, bool S32, bool DIAG>
 __global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_multi_kernel(MultiDrawParams mp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    DrawWarp<RMAX, float> dw;
-    setup_draw_warp<RMAX, float>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+    DrawWarp<RMAX, float, DIAG> dw;
+    setup_draw_warp<RMAX, float, DIAG>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t total = mp.cum[mp.n];
     const int64_t nw = (int64_t)gridDim.x * Blk<RMAX, float>::WARPS;
@@ -260,7 +268,7 @@ __global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_multi_
             const int src = __ffs(bal) - 1;
             bal &= bal - 1;
             const int rs = __shfl_sync(0xffffffffu, r, src);
-            draw_sample<RMAX, float, true, S32>(mp.req[rs], b + src - mp.cum[rs], dw);
+            draw_sample<RMAX, float, true, S32, DIAG>(mp.req[rs], b + src - mp.cum[rs], dw);
         }
     }
 }
@@ -279,8 +287,8 @@ struct TreeSampleParams {
 
 // PartitionTree::PTSample_internal (cpp_ext/partition_tree.hpp:232-405):
 // x = scaled_h[i]; samples[i] = selected row; h[i] o= U[row].
-template <int RMAX, typename T>
-__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FTL_DESC_RESIDENT_F32 : FTL_DESC_RESIDENT_F64) / (Blk<RMAX, T>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
+template <int RMAX, typename T, bool DIAG>
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T>::WARPS * 32)) tree_sample_kernel(TreeSampleParams p) {
     using S = Shape<RMAX>;
     constexpr int XPL = S::XPL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -290,10 +298,10 @@ __global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, (sizeof(T) == 4 ? FT
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char *slot = smem_raw + ((NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16) +
-                          warp * WarpSlot<RMAX, T>::bytes;
+                          warp * WarpSlot<RMAX, T, DIAG>::bytes;
     double *xd = (double *)slot;
     T *xT = sizeof(T) == 8 ? (T *)xd : (T *)(xd + RMAX);
-    QForm<RMAX, T> qf;
+    typename QSel<RMAX, T, DIAG>::type qf;
     qf.P = P;
     qf.S = p.S;
     qf.s = (T *)(slot + RMAX * sizeof(double) + RMAX * sizeof(T));
@@ -346,70 +354,70 @@ __global__ void philox_fill_kernel(double *out, int64_t n, uint64_t seed, uint64
         out[i] = philox_uniform(seed, ctr + (uint64_t)i);
 }
 
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool DIAG = false>
 static size_t desc_smem() {
     return (NodeShape<RMAX, T>::SMAX * sizeof(uint16_t) + 15) / 16 * 16 +
-           (size_t)Blk<RMAX, T>::WARPS * WarpSlot<RMAX, T>::bytes;
+           (size_t)Blk<RMAX, T>::WARPS * WarpSlot<RMAX, T, DIAG>::bytes;
 }
 
-template <int RMAX, typename T, bool S32>
+template <int RMAX, typename T, bool S32, bool DIAG>
 static int launch_draw(const DrawParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
-    size_t smem = desc_smem<RMAX, T>();
+    size_t smem = desc_smem<RMAX, T, DIAG>();
     {
-        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32>, smem, "krp_draw_kernel");
+        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32, DIAG>, smem, "krp_draw_kernel");
         if (arc) return arc;
     }
     int64_t blocks = (p.J + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_kernel<RMAX, T, S32><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
+    krp_draw_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     int rc = check_launch("krp_draw_kernel");
     if (rc || sizeof(T) == 8) return rc;
     {
-        const int arc = ensure_smem((const void *)krp_fixup_kernel<RMAX, S32>, smem, "krp_fixup_kernel");
+        const int arc = ensure_smem((const void *)krp_fixup_kernel<RMAX, S32, DIAG>, smem, "krp_fixup_kernel");
         if (arc) return arc;
     }
     int64_t fblocks = (p.J + 32 * warps - 1) / (32 * warps);
     fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
-    krp_fixup_kernel<RMAX, S32><<<(unsigned)fblocks, warps * 32, smem, st>>>(p);
+    krp_fixup_kernel<RMAX, S32, DIAG><<<(unsigned)fblocks, warps * 32, smem, st>>>(p);
     return check_launch("krp_fixup_kernel");
 }
 
-template <int RMAX, typename T, bool S32>
+template <int RMAX, typename T, bool S32, bool DIAG>
 static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
-    size_t smem = desc_smem<RMAX, T>();
+    size_t smem = desc_smem<RMAX, T, DIAG>();
     {
-        const int arc = ensure_smem((const void *)krp_draw_multi_kernel<RMAX, T, S32>, smem, "krp_draw_multi_kernel");
+        const int arc = ensure_smem((const void *)krp_draw_multi_kernel<RMAX, T, S32, DIAG>, smem, "krp_draw_multi_kernel");
         if (arc) return arc;
     }
     const int64_t total = mp.cum[mp.n];
     int64_t blocks = (total + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_multi_kernel<RMAX, T, S32><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
+    krp_draw_multi_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
     int rc = check_launch("krp_draw_multi_kernel");
     if (rc || sizeof(T) == 8) return rc;
     {
-        const int arc = ensure_smem((const void *)krp_fixup_multi_kernel<RMAX, S32>, smem, "krp_fixup_multi_kernel");
+        const int arc = ensure_smem((const void *)krp_fixup_multi_kernel<RMAX, S32, DIAG>, smem, "krp_fixup_multi_kernel");
         if (arc) return arc;
     }
     int64_t fblocks = (total + 32 * warps - 1) / (32 * warps);
     fblocks = std::max<int64_t>(1, std::min<int64_t>(fblocks, (int64_t)num_sms() * 8));
-    krp_fixup_multi_kernel<RMAX, S32><<<(unsigned)fblocks, warps * 32, smem, st>>>(mp);
+    krp_fixup_multi_kernel<RMAX, S32, DIAG><<<(unsigned)fblocks, warps * 32, smem, st>>>(mp);
     return check_launch("krp_fixup_multi_kernel");
 }
 
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool DIAG>
 static int launch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
-    size_t smem = desc_smem<RMAX, T>();
+    size_t smem = desc_smem<RMAX, T, DIAG>();
     {
-        const int arc = ensure_smem((const void *)tree_sample_kernel<RMAX, T>, smem, "tree_sample_kernel");
+        const int arc = ensure_smem((const void *)tree_sample_kernel<RMAX, T, DIAG>, smem, "tree_sample_kernel");
         if (arc) return arc;
     }
     int64_t blocks = (p.J + warps - 1) / warps;
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    tree_sample_kernel<RMAX, T><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
+    tree_sample_kernel<RMAX, T, DIAG><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     return check_launch("tree_sample_kernel");
 }
 
@@ -424,14 +432,19 @@ static bool shadows_ready(const DrawParams &p) {
 
 template <typename T>
 static int dispatch_draw(const DrawParams &p, cudaStream_t st) {
-    if (sizeof(T) == 4 && shadows_ready(p)) {
-        if (p.R <= 32) return launch_draw<32, T, true>(p, st);
-        if (p.R <= 64) return launch_draw<64, T, true>(p, st);
-        return launch_draw<128, T, true>(p, st);
+    if constexpr (sizeof(T) == 4) {
+        const bool diag = node_layout(p.R, sizeof(T)) == FTL_LAYOUT_DIAG32;
+        if (shadows_ready(p)) {
+            if (diag) return launch_draw<32, T, true, true>(p, st);
+            if (p.R <= 32) return launch_draw<32, T, true, false>(p, st);
+            if (p.R <= 64) return launch_draw<64, T, true, false>(p, st);
+            return launch_draw<128, T, true, false>(p, st);
+        }
+        if (diag) return launch_draw<32, T, false, true>(p, st);
     }
-    if (p.R <= 32) return launch_draw<32, T, false>(p, st);
-    if (p.R <= 64) return launch_draw<64, T, false>(p, st);
-    return launch_draw<128, T, false>(p, st);
+    if (p.R <= 32) return launch_draw<32, T, false, false>(p, st);
+    if (p.R <= 64) return launch_draw<64, T, false, false>(p, st);
+    return launch_draw<128, T, false, false>(p, st);
 }
 
 // The register/shared-memory shapes are chosen by max(R, F): a lane handles
@@ -439,9 +452,11 @@ static int dispatch_draw(const DrawParams &p, cudaStream_t st) {
 template <typename T>
 static int dispatch_tree_sample(const TreeSampleParams &p, cudaStream_t st) {
     const int64_t RF = std::max<int64_t>(p.R, p.g.F);
-    if (RF <= 32) return launch_tree_sample<32, T>(p, st);
-    if (RF <= 64) return launch_tree_sample<64, T>(p, st);
-    return launch_tree_sample<128, T>(p, st);
+    if constexpr (sizeof(T) == 4)
+        if (node_layout(p.R, sizeof(T)) == FTL_LAYOUT_DIAG32 && RF <= 32) return launch_tree_sample<32, T, true>(p, st);
+    if (RF <= 32) return launch_tree_sample<32, T, false>(p, st);
+    if (RF <= 64) return launch_tree_sample<64, T, false>(p, st);
+    return launch_tree_sample<128, T, false>(p, st);
 }
 
 static int validate_plan(const ftl_krp_plan *plan) {
@@ -476,8 +491,8 @@ extern "C" int ftl_krp_plan_sizes(int N, int R, int prec, size_t *eig_bytes, siz
                                   size_t *lambda_bytes, size_t *pinv32_bytes) {
     FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES && R >= 1 && R <= FTL_MAX_RANK,
                   "ftl_krp_plan_sizes: bad N=%d R=%d", N, R);
-    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_krp_plan_sizes: bad precision");
-    const int esize = prec == FTL_PREC_FP64 ? 8 : 4;
+    FTL_CHECK_ARG(valid_prec(prec), "ftl_krp_plan_sizes: bad precision");
+    const int esize = prec_bytes(prec);
     if (eig_bytes) *eig_bytes = (size_t)N * (2 * R - 1) * node_stride(R, esize) * esize;
     if (M_bytes) *M_bytes = (cm_pinv64_offset(N, R) + node_stride(R, 8)) * sizeof(double);
     if (lambda_bytes) *lambda_bytes = (size_t)(N + 1) * R * sizeof(double);
@@ -570,20 +585,23 @@ extern "C" int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, co
     cudaStream_t st = (cudaStream_t)stream;
     const int R = plans[0]->R;
     if (plans[0]->prec == FTL_PREC_FP64) {
-        if (R <= 32) return launch_multi<32, double, false>(mp, st);
-        if (R <= 64) return launch_multi<64, double, false>(mp, st);
-        return launch_multi<128, double, false>(mp, st);
+        if (R <= 32) return launch_multi<32, double, false, false>(mp, st);
+        if (R <= 64) return launch_multi<64, double, false, false>(mp, st);
+        return launch_multi<128, double, false, false>(mp, st);
     }
     bool s32 = true;
     for (int i = 0; i < n; ++i) s32 = s32 && shadows_ready(mp.req[i]);
+    const bool diag = node_layout(R, 4) == FTL_LAYOUT_DIAG32;
     if (s32) {
-        if (R <= 32) return launch_multi<32, float, true>(mp, st);
-        if (R <= 64) return launch_multi<64, float, true>(mp, st);
-        return launch_multi<128, float, true>(mp, st);
+        if (diag) return launch_multi<32, float, true, true>(mp, st);
+        if (R <= 32) return launch_multi<32, float, true, false>(mp, st);
+        if (R <= 64) return launch_multi<64, float, true, false>(mp, st);
+        return launch_multi<128, float, true, false>(mp, st);
     }
-    if (R <= 32) return launch_multi<32, float, false>(mp, st);
-    if (R <= 64) return launch_multi<64, float, false>(mp, st);
-    return launch_multi<128, float, false>(mp, st);
+    if (diag) return launch_multi<32, float, false, true>(mp, st);
+    if (R <= 32) return launch_multi<32, float, false, false>(mp, st);
+    if (R <= 64) return launch_multi<64, float, false, false>(mp, st);
+    return launch_multi<128, float, false, false>(mp, st);
 }
 
 extern "C" int ftl_krp_draw(const ftl_krp_plan *plan, uint32_t j, uint64_t *samples, double *h,
@@ -608,7 +626,9 @@ extern "C" int ftl_tree_sample(const void *G, int prec, const double *U, int64_t
     p.U = U;
     p.R = R;
     p.P = packed_size(R);
-    p.S = node_stride(R, prec == FTL_PREC_FP64 ? 8 : 4);
+    FTL_CHECK_ARG(valid_prec(prec), "ftl_tree_sample: bad precision %d", prec);
+    prec = storage_prec(prec);
+    p.S = node_stride(R, prec_bytes(prec));
     p.g = to_dgeom(make_geom(n, F));
     p.h = h;
     p.scaled_h = scaled_h;

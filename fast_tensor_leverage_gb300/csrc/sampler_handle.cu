@@ -3,7 +3,7 @@
 // workspaces (the state of EfficientKRPSampler, efficient_krp_sampler.hpp:
 // 32-75), so a caller needs four calls: create, set_factor per mode, draw,
 // destroy.  Everything below is host code over the plan-based entry points
-// (ftl_tree_build, ftl_factor_shadow, ftl_krp_draw); the device work is the
+// (ftl_tree_build_ex, ftl_krp_draw); the device work is the
 // same.  Unlike those entry points, create allocates (cudaMalloc) and destroy
 // frees.
 #include <cstring>
@@ -13,6 +13,7 @@
 
 struct ftl_sampler {
     ftl_krp_plan plan;
+    int tree_prec;  // FTL_PREC_* the trees are built with (plan.prec is its node precision)
     int64_t F[FTL_MAX_MODES];
     std::vector<void *> owned;  // every cudaMalloc of this handle, freed by destroy
 };
@@ -51,7 +52,7 @@ extern "C" int ftl_sampler_create(int N, const int64_t *dims, int R, int64_t J, 
     FTL_CHECK_ARG(N >= 1 && N <= FTL_MAX_MODES, "ftl_sampler_create: N=%d outside 1..%d", N, FTL_MAX_MODES);
     FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK, "ftl_sampler_create: R=%d outside 1..%d", R, FTL_MAX_RANK);
     FTL_CHECK_ARG(J >= 1, "ftl_sampler_create: J=%lld", (long long)J);
-    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_sampler_create: bad precision %d", prec);
+    FTL_CHECK_ARG(ftl::valid_prec(prec), "ftl_sampler_create: bad precision %d", prec);
     for (int k = 0; k < N; ++k)
         FTL_CHECK_ARG(dims[k] >= 1, "ftl_sampler_create: dims[%d]=%lld", k, (long long)dims[k]);
     ftl_sampler *s = new ftl_sampler();
@@ -60,7 +61,8 @@ extern "C" int ftl_sampler_create(int N, const int64_t *dims, int R, int64_t J, 
     p.N = N;
     p.R = R;
     p.J = J;
-    p.prec = prec;
+    p.prec = ftl::storage_prec(prec);  // the draws see FP64 or FP32 nodes
+    s->tree_prec = prec;
     int rc = FTL_OK;
     for (int k = 0; k < N && rc == FTL_OK; ++k) {
         p.dims[k] = dims[k];
@@ -72,7 +74,7 @@ extern "C" int ftl_sampler_create(int N, const int64_t *dims, int R, int64_t J, 
         if (rc == FTL_OK) rc = alloc(s, tb, &g, true);
         p.U[k] = (const double *)u;
         p.gram_G[k] = g;
-        if (rc == FTL_OK && factor_shadows && prec == FTL_PREC_FP32) {
+        if (rc == FTL_OK && factor_shadows && prec != FTL_PREC_FP64) {
             void *u32 = nullptr;
             rc = alloc(s, (size_t)dims[k] * R * sizeof(float), &u32, true);
             p.U32[k] = (const float *)u32;
@@ -114,10 +116,8 @@ extern "C" int ftl_sampler_update(ftl_sampler *s, int k, void *stream) {
     FTL_CHECK_ARG(s, "ftl_sampler_update: null pointer");
     FTL_CHECK_ARG(k >= 0 && k < s->plan.N, "ftl_sampler_update: k=%d outside 0..%d", k, s->plan.N - 1);
     ftl_krp_plan &p = s->plan;
-    int rc = ftl_tree_build(p.U[k], p.dims[k], p.R, s->F[k], p.prec, p.gram_G[k], stream);
-    if (rc == FTL_OK && p.U32[k])
-        rc = ftl_factor_shadow(p.U[k], p.dims[k] * p.R, (float *)p.U32[k], stream);
-    return rc;
+    // the tree and the FP32 copy of the factor (when kept) in one pass
+    return ftl_tree_build_ex(p.U[k], p.dims[k], p.R, s->F[k], s->tree_prec, p.gram_G[k], (float *)p.U32[k], stream);
 }
 
 extern "C" int ftl_sampler_factor(const ftl_sampler *s, int k, double **U_dev) {

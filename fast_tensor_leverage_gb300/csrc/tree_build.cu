@@ -32,9 +32,15 @@ struct Vec4<double> {
 };
 
 template <typename T>
+__device__ __forceinline__ T to_tree(double x) {
+    if constexpr (sizeof(T) == 4) return d2f_rn(x);
+    else return x;
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict__ U, int64_t n,
                                                         int R, int RP, DGeom g, int LB,
-                                                        T *__restrict__ G) {
+                                                        T *__restrict__ G, float *__restrict__ U32) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     T *Us = reinterpret_cast<T *>(smem_raw);  // LB x F x RP
     const int64_t F = g.F;
@@ -58,11 +64,25 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
             const int64_t row = row0 + rr;
             for (int col = lane; col < RP; col += 32) {
                 T v = T(0);
-                if (row < n && col < R) v = (T)U[row * R + col];
+                if (row < n && col < R) {
+                    v = to_tree<T>(U[row * R + col]);
+                    if (sizeof(T) == 4 && U32) U32[row * R + col] = (float)v;  // the FP32 copy, same pass
+                }
                 Us[rr * RP + col] = v;
             }
         }
         __syncthreads();
+        const int lay = node_layout(R, sizeof(T));
+        if (lay == FTL_LAYOUT_DIAG32 && R < 32) {
+            // entries of the 32 x 32 padding outside the R x R Gram are zero
+            for (int w = threadIdx.x; w < LB * S; w += blockDim.x) {
+                const int lb = w / S, e = w - lb * S;
+                const int64_t leaf = leaf0 + lb;
+                int a, b;
+                diag32_entry(e, a, b);
+                if (leaf < leaf_count && (a >= R || b >= R)) G[leaf_node(g, leaf) * (int64_t)S + e] = T(0);
+            }
+        }
         const int work = LB * tiles;
         for (int w = threadIdx.x; w < work; w += blockDim.x) {
             int lb = w / tiles;
@@ -95,7 +115,7 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
                     for (int y = 0; y < 4; ++y) acc[x][y] = fma(a4[x], b4[y], acc[x][y]);
             }
             T *Gn = G + leaf_node(g, leaf) * (int64_t)S;
-            if (tile == 0)
+            if (tile == 0 && lay == FTL_LAYOUT_PACKED)
                 for (int e = P; e < S; ++e) Gn[e] = T(0);
 #pragma unroll
             for (int x = 0; x < 4; ++x) {
@@ -105,7 +125,12 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
                 for (int y = 0; y < 4; ++y) {
                     int b = 4 * tb + y;
                     if (b < a || b >= R) continue;
-                    Gn[packed_index(a, b, R)] = acc[x][y];
+                    if (lay == FTL_LAYOUT_DIAG32) {
+                        Gn[diag32_pos(a, b)] = acc[x][y];
+                        if (((b - a) & 31) == 16) Gn[512 + b] = acc[x][y];  // the second copy
+                    } else {
+                        Gn[packed_index(a, b, R)] = acc[x][y];
+                    }
                 }
             }
         }
@@ -173,19 +198,39 @@ static void launch_fused(V *G, int64_t top_start, int64_t top_count, int S16, cu
 
 template <typename T>
 __global__ void tree_scale_kernel(const T *__restrict__ src, T *__restrict__ dst, int64_t total,
-                                  int P, int S, const double *__restrict__ mat) {
+                                  int R, int P, int S, const double *__restrict__ mat) {
+    const bool diag = node_layout(R, sizeof(T)) == FTL_LAYOUT_DIAG32;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         int k = (int)(e % S);
-        dst[e] = k < P ? (T)((double)src[e] * mat[k]) : T(0);
+        if (diag) {
+            int a, b;
+            diag32_entry(k, a, b);
+            dst[e] = (a < R && b < R) ? (T)((double)src[e] * mat[packed_index(min(a, b), max(a, b), R)]) : T(0);
+        } else {
+            dst[e] = k < P ? (T)((double)src[e] * mat[k]) : T(0);
+        }
     }
 }
 
 
+int tc_leaf_grams(const double *U, int64_t n, int R, int64_t F, int mode, float *G, float *U32, cudaStream_t st);
+
 template <typename T>
-static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaStream_t st) {
+static int build_internal(const Geom &geom, int R, T *G, cudaStream_t st);
+
+// prec: FTL_PREC_FP64 (T = double) or one of the FP32-node precisions.
+template <typename T>
+static int build_impl(const double *U, int64_t n, int R, int64_t F, int prec, T *G, float *U32, cudaStream_t st) {
     Geom geom = make_geom(n, F);
     DGeom g = to_dgeom(geom);
+    int rc = FTL_OK;
+    if (sizeof(T) == 4 && (prec == FTL_PREC_TF32X3 || prec == FTL_PREC_BF16) && F <= R && R <= 32 &&
+        n < ((int64_t)1 << 31)) {
+        rc = tc_leaf_grams(U, n, R, F, prec == FTL_PREC_TF32X3 ? 0 : 1, (float *)G, U32, st);
+        if (rc) return rc;
+        return build_internal<T>(geom, R, G, st);
+    }
     const int P = packed_size(R);
     const int RP = (R + 3) / 4 * 4;
     const size_t blk_bytes = (size_t)F * RP * sizeof(T);
@@ -198,7 +243,7 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     if (smem > 227 * 1024)
         return fail(FTL_E_UNSUPPORTED, "tree_build: leaf block of %lld x %d needs %zu B of shared memory",
                     (long long)F, R, smem);
-    int rc = ensure_smem((const void *)leaf_gram_kernel<T>, smem, "leaf_gram_kernel");
+    rc = ensure_smem((const void *)leaf_gram_kernel<T>, smem, "leaf_gram_kernel");
     if (rc) return rc;
     int64_t nbatch = (geom.leaf_count + LB - 1) / LB;
     // one wave of resident CTAs, each looping over batches: a grid larger
@@ -207,9 +252,16 @@ static int build_impl(const double *U, int64_t n, int R, int64_t F, T *G, cudaSt
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_gram_kernel<T>, 256, smem) != cudaSuccess || occ < 1)
         occ = 1;
     int grid = (int)std::min<int64_t>(nbatch, (int64_t)num_sms() * occ);
-    leaf_gram_kernel<T><<<grid, 256, smem, st>>>(U, n, R, RP, g, LB, G);
+    leaf_gram_kernel<T><<<grid, 256, smem, st>>>(U, n, R, RP, g, LB, G, U32);
     rc = check_launch("leaf_gram_kernel");
     if (rc) return rc;
+    return build_internal<T>(geom, R, G, st);
+}
+
+// Internal nodes of a tree whose leaves are built: parent = left + right.
+template <typename T>
+static int build_internal(const Geom &geom, int R, T *G, cudaStream_t st) {
+    int rc = FTL_OK;
     using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
     const int S16 = node_stride(R, sizeof(T)) * (int)sizeof(T) / 16;
     // internal nodes of the partial level (children: leaves of the last level)
@@ -268,43 +320,64 @@ extern "C" int ftl_tree_geometry(int64_t n, int64_t F, ftl_tree_geom *out) {
     return FTL_OK;
 }
 
+extern "C" int ftl_node_layout(int R, int prec, int *layout_out, int *stride_out, int32_t *pos_out) {
+    FTL_CHECK_ARG(R >= 1 && R <= FTL_MAX_RANK, "ftl_node_layout: R=%d outside [1, %d]", R, FTL_MAX_RANK);
+    FTL_CHECK_ARG(valid_prec(prec), "ftl_node_layout: bad precision %d", prec);
+    const int esize = prec_bytes(prec);
+    if (layout_out) *layout_out = node_layout(R, esize);
+    if (stride_out) *stride_out = node_stride(R, esize);
+    if (pos_out) {
+        int e = 0;
+        for (int a = 0; a < R; ++a)
+            for (int b = a; b < R; ++b) pos_out[e++] = node_pos(a, b, R, esize);
+    }
+    return FTL_OK;
+}
+
 extern "C" int ftl_tree_bytes(int64_t n, int64_t F, int R, int prec, size_t *out_bytes) {
     FTL_CHECK_ARG(out_bytes != nullptr, "ftl_tree_bytes: out_bytes is NULL");
     FTL_CHECK_ARG(n >= 1 && F >= 1 && R >= 1 && R <= FTL_MAX_RANK,
                   "ftl_tree_bytes: bad shape n=%lld F=%lld R=%d", (long long)n, (long long)F, R);
-    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_tree_bytes: bad precision %d", prec);
+    FTL_CHECK_ARG(valid_prec(prec), "ftl_tree_bytes: bad precision %d", prec);
     Geom g = make_geom(n, F);
-    const int esize = prec == FTL_PREC_FP64 ? 8 : 4;
+    const int esize = prec_bytes(prec);
     *out_bytes = (size_t)g.node_count * node_stride(R, esize) * esize;
     return FTL_OK;
 }
 
-extern "C" int ftl_tree_build(const double *U, int64_t n, int R, int64_t F, int prec, void *G,
-                              void *stream) {
+extern "C" int ftl_tree_build_ex(const double *U, int64_t n, int R, int64_t F, int prec, void *G, float *U32,
+                                 void *stream) {
     FTL_CHECK_ARG(U != nullptr && G != nullptr, "ftl_tree_build: null pointer");
     FTL_CHECK_ARG(n >= 1 && F >= 1 && R >= 1 && R <= FTL_MAX_RANK,
                   "ftl_tree_build: bad shape n=%lld F=%lld R=%d", (long long)n, (long long)F, R);
     FTL_CHECK_ARG(F <= FTL_MAX_RANK, "ftl_tree_build: F=%lld exceeds %d", (long long)F, FTL_MAX_RANK);
     FTL_CHECK_ARG(aligned16(G), "ftl_tree_build: the tree must be 16-byte aligned");
+    FTL_CHECK_ARG(valid_prec(prec), "ftl_tree_build: bad precision %d", prec);
+    FTL_CHECK_ARG(U32 == nullptr || prec != FTL_PREC_FP64, "ftl_tree_build: FP32 factor copies need an FP32 tree");
     cudaStream_t st = (cudaStream_t)stream;
-    if (prec == FTL_PREC_FP64) return build_impl<double>(U, n, R, F, (double *)G, st);
-    if (prec == FTL_PREC_FP32) return build_impl<float>(U, n, R, F, (float *)G, st);
-    return fail(FTL_E_ARG, "ftl_tree_build: bad precision %d", prec);
+    if (prec == FTL_PREC_FP64) return build_impl<double>(U, n, R, F, prec, (double *)G, nullptr, st);
+    return build_impl<float>(U, n, R, F, prec, (float *)G, U32, st);
+}
+
+extern "C" int ftl_tree_build(const double *U, int64_t n, int R, int64_t F, int prec, void *G,
+                              void *stream) {
+    return ftl_tree_build_ex(U, n, R, F, prec, G, nullptr, stream);
 }
 
 extern "C" int ftl_tree_scale(const void *G_src, void *G_dst, int64_t node_count, int R, int prec,
                               const double *mat, void *stream) {
     FTL_CHECK_ARG(G_src && G_dst && mat, "ftl_tree_scale: null pointer");
     FTL_CHECK_ARG(node_count >= 1 && R >= 1 && R <= FTL_MAX_RANK, "ftl_tree_scale: bad shape");
-    FTL_CHECK_ARG(prec == FTL_PREC_FP64 || prec == FTL_PREC_FP32, "ftl_tree_scale: bad precision %d", prec);
+    FTL_CHECK_ARG(valid_prec(prec), "ftl_tree_scale: bad precision %d", prec);
+    prec = storage_prec(prec);
     const int P = packed_size(R);
-    const int S = node_stride(R, prec == FTL_PREC_FP64 ? 8 : 4);
+    const int S = node_stride(R, prec_bytes(prec));
     int64_t total = node_count * (int64_t)S;
     int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
     cudaStream_t st = (cudaStream_t)stream;
     if (prec == FTL_PREC_FP64)
-        tree_scale_kernel<double><<<blocks, 256, 0, st>>>((const double *)G_src, (double *)G_dst, total, P, S, mat);
+        tree_scale_kernel<double><<<blocks, 256, 0, st>>>((const double *)G_src, (double *)G_dst, total, R, P, S, mat);
     else
-        tree_scale_kernel<float><<<blocks, 256, 0, st>>>((const float *)G_src, (float *)G_dst, total, P, S, mat);
+        tree_scale_kernel<float><<<blocks, 256, 0, st>>>((const float *)G_src, (float *)G_dst, total, R, P, S, mat);
     return check_launch("tree_scale_kernel");
 }

@@ -32,7 +32,7 @@ class PartitionTree:
         self.P = R * (R + 1) // 2
         dt = torch.float64 if precision == "fp64" else torch.float32
         nbytes = _lib.tree_bytes(n, F, R, self._prec)
-        self.S = nbytes // (self.node_count * dt.itemsize)  # node stride (16-byte padded)
+        self.S = nbytes // (self.node_count * dt.itemsize)  # values per node (ftl_node_layout)
         self.G = torch.zeros(nbytes // dt.itemsize, dtype=dt, device=self.device)
         self._G_unmultiplied = None
         self._U = None
@@ -63,14 +63,17 @@ class PartitionTree:
         """Root Gram into out (R x R): upper triangle, zero lower triangle, as
         the reference stores it (partition_tree.hpp:172-177)."""
         o = D.require_numpy_out(out, np.float64, "out", min_size=self.R * self.R)
-        root = self.G[: self.P].double().cpu().numpy()
+        _, _, pos = _lib.node_layout(self.R, self._prec)
+        root = self.G[: self.S].double().cpu().numpy()[pos]
         full = np.zeros((self.R, self.R))
         full[np.triu_indices(self.R)] = root
         o.reshape(-1)[: self.R * self.R] = full.reshape(-1)
 
     def get_G(self) -> np.ndarray:
-        """All node Grams as packed upper triangles, (node_count, P)."""
-        return self.G.double().cpu().numpy().reshape(self.node_count, self.S)[:, : self.P].copy()
+        """All node Grams as packed upper triangles, (node_count, P), whatever
+        the device layout."""
+        _, _, pos = _lib.node_layout(self.R, self._prec)
+        return self.G.double().cpu().numpy().reshape(self.node_count, self.S)[:, pos].copy()
 
     def PTSample(self, U, h, scaled_h, samples, random_draws) -> None:
         """PartitionTree::PTSample (partition_tree.hpp:216-405): for every row

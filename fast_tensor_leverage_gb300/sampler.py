@@ -46,6 +46,7 @@ class Sampler:
         self.dims = [int(f.shape[0]) for f in factors]
         self.F = [min(R, n) for n in self.dims]
         self.P = R * (R + 1) // 2
+        self._plan_prec = _lib.storage_prec(self._prec)   # what the draws see
         tdt = torch.float64 if precision == "fp64" else torch.float32
         dev = self.device
         self.U = [f.to(dev, torch.float64).contiguous() if isinstance(f, torch.Tensor)
@@ -53,7 +54,7 @@ class Sampler:
         # FP32 mode: FP32 copies of the factors for the leaf scans (half the
         # leaf-block bytes, same results); refreshed with each tree
         self.U32 = ([torch.empty((n, R), dtype=torch.float32, device=dev) for n in self.dims]
-                    if precision == "fp32" and factor_shadows else None)
+                    if precision != "fp64" and factor_shadows else None)
         self.trees = []
         for k in range(N):
             nb = _lib.tree_bytes(self.dims[k], self.F[k], R, self._prec)
@@ -113,7 +114,7 @@ class Sampler:
     # ----------------------------------------------------------- plumbing
     def _refresh_plan(self) -> None:
         for p, (eig, M, lam, p32) in zip(self._plans, self._ws_sets):
-            p.N, p.R, p.J, p.prec = self.N, self.R, self.J, self._prec
+            p.N, p.R, p.J, p.prec = self.N, self.R, self.J, self._plan_prec
             for k in range(self.N):
                 p.dims[k] = self.dims[k]
                 p.U[k] = self.U[k].data_ptr()
@@ -137,11 +138,11 @@ class Sampler:
             main = stream if stream is not None else torch.cuda.current_stream(self.device)
             main.wait_event(self._cm_done[self._spec[0]])
             self._spec = None
-        _lib.call("ftl_tree_build", self.U[j].data_ptr(), self.dims[j], self.R, self.F[j],
-                  self._prec, self.trees[j].data_ptr(), self._stream(stream))
-        if self.U32 is not None:
-            _lib.call("ftl_factor_shadow", self.U[j].data_ptr(), self.dims[j] * self.R, self.U32[j].data_ptr(),
-                      self._stream(stream))
+        # the tree and (FP32 trees with copies) the FP32 copy of the factor
+        # for the leaf scans, in one pass over the factor
+        _lib.call("ftl_tree_build_ex", self.U[j].data_ptr(), self.dims[j], self.R, self.F[j],
+                  self._prec, self.trees[j].data_ptr(),
+                  self.U32[j].data_ptr() if self.U32 is not None else None, self._stream(stream))
         # computeM on the side stream must see this tree
         self._tree_ev.record(stream if stream is not None else torch.cuda.current_stream(self.device))
 
@@ -279,19 +280,16 @@ class Sampler:
     def weights(self) -> np.ndarray:
         return self.weights_dev.cpu().numpy()
 
-    def _stride(self) -> int:
-        w = 16 // (8 if self.precision == "fp64" else 4)
-        return (self.P + w - 1) // w * w
-
     def gram_tree(self, k: int) -> np.ndarray:
-        """Node Grams of factor k's tree, (node_count, P) packed, as FP64."""
-        S = self._stride()
-        return self.trees[k].double().cpu().numpy().reshape(-1, S)[:, : self.P].copy()
+        """Node Grams of factor k's tree, (node_count, P) packed upper
+        triangles (whatever the device layout), as FP64."""
+        _, S, pos = _lib.node_layout(self.R, self._plan_prec)
+        return self.trees[k].double().cpu().numpy().reshape(-1, S)[:, pos].copy()
 
     def eigen_tree(self, k: int) -> np.ndarray:
-        S = self._stride()
+        _, S, pos = _lib.node_layout(self.R, self._plan_prec)
         e = self.eig_G.double().cpu().numpy().reshape(self.N, 2 * self.R - 1, S)
-        return e[k, :, : self.P].copy()
+        return e[k][:, pos].copy()
 
     def workspace_M(self) -> np.ndarray:
         return self.M.cpu().numpy().reshape(-1, self.R, self.R)

@@ -10,9 +10,17 @@
  *     here frees caller memory.  `stream` is a cudaStream_t passed as void*
  *     (NULL = legacy default stream).  Calls are asynchronous on `stream`
  *     unless stated otherwise.
- *   - Matrices are row-major, contiguous.  Node Gram matrices are stored as
- *     packed upper triangles: element (a,b), a <= b, of an R x R Gram lives
- *     at a*R - a*(a-1)/2 + (b-a); P = R*(R+1)/2 values per node.
+ *   - Matrices are row-major, contiguous.  Node Gram matrices are stored in
+ *     one of two layouts (ftl_node_layout tells which, with the position of
+ *     every element):
+ *       PACKED (FTL_LAYOUT_PACKED; FP64 nodes, FP32 nodes with R <= 16 or
+ *       R > 32): the upper triangle, element (a,b), a <= b, at
+ *       a*R - a*(a-1)/2 + (b-a); P = R*(R+1)/2 values, zero padded to 16 bytes.
+ *       DIAG32 (FTL_LAYOUT_DIAG32; FP32 nodes with 16 < R <= 32): the Gram
+ *       zero padded to 32 x 32, stored by wrapped diagonals so that lane a
+ *       of a warp reads row a with coalesced loads: G[a][(a+d) mod 32] at
+ *       ((d/4)*32 + a)*4 + d%4 for d = 0..15, and G[a][(a+16) mod 32] at
+ *       512 + a (those entries twice, once from each end); 544 values.
  *   - Tree node numbering, leaf numbering and the descent arithmetic follow
  *     the reference's PartitionTree exactly (heap order, children 2c+1 and
  *     2c+2, partial deepest level first).
@@ -47,6 +55,13 @@ extern "C" {
  * the running draw offset kept in double-float. */
 #define FTL_PREC_FP64 0
 #define FTL_PREC_FP32 1
+/* Tree-build precisions with FP32 nodes (plans and draws treat these trees
+ * as FTL_PREC_FP32).  For F <= R <= 32 the leaf Grams run on the tensor
+ * cores (tcgen05, TMA-fed) with FP32 accumulation, from the factor rows split
+ * as 3xTF32 (hi*hi + hi*lo + lo*hi, about FP32 accuracy) or rounded to BF16;
+ * for larger R they fall back to the FP32 CUDA-core build. */
+#define FTL_PREC_TF32X3 2
+#define FTL_PREC_BF16 3
 
 #define FTL_MAX_MODES 16
 #define FTL_MAX_RANK 128
@@ -76,12 +91,21 @@ typedef struct ftl_tree_geom {
  * cpp_ext/partition_tree.hpp:83-105 (log2_round_down: cpp_ext/common.h:21-33). */
 int ftl_tree_geometry(int64_t n, int64_t F, ftl_tree_geom *out);
 
+/* Node layout of an R-column Gram in precision prec: *layout_out =
+ * FTL_LAYOUT_PACKED or FTL_LAYOUT_DIAG32, *stride_out = values per node, and
+ * (pos_out, P = R*(R+1)/2 entries, may be NULL) the position inside a node of
+ * upper-triangle element number e (row-major order over a <= b).  No
+ * counterpart in the reference (it stores full R x R matrices). */
+#define FTL_LAYOUT_PACKED 0
+#define FTL_LAYOUT_DIAG32 1
+int ftl_node_layout(int R, int prec, int *layout_out, int *stride_out, int32_t *pos_out);
+
 /* Bytes of one tree's node array: node_count * node_stride * (8 for FP64, 4 for FP32). */
 int ftl_tree_bytes(int64_t n, int64_t F, int R, int prec, size_t *out_bytes);
 
 /* Node arrays (trees, eigen trees) and the computeM workspaces must be
  * 16-byte aligned: nodes are read with 16-byte loads.  Each node occupies
- * node_stride = P rounded up to 16 bytes (2 doubles / 4 floats), zero padded. */
+ * node_stride values (ftl_node_layout), zero padded. */
 
 /* Build the node Grams of the tree over U_dev (n x R, FP64): each leaf holds
  * U_blk^T U_blk of its <= F rows, each internal node the sum of its children.
@@ -89,6 +113,17 @@ int ftl_tree_bytes(int64_t n, int64_t F, int R, int prec, size_t *out_bytes);
  * Replaces PartitionTree::build_tree, cpp_ext/partition_tree.hpp:120-170. */
 int ftl_tree_build(const double *U_dev, int64_t n, int R, int64_t F, int prec,
                    void *G_dev, void *stream);
+
+/* ftl_tree_build that also writes U32_dev (n x R FP32, may be NULL; not for
+ * FP64 trees) = U rounded to FP32, the copy FP32 draws read their leaf blocks
+ * from, in the same pass over U.  No counterpart in the reference. */
+int ftl_tree_build_ex(const double *U_dev, int64_t n, int R, int64_t F, int prec,
+                      void *G_dev, float *U32_dev, void *stream);
+
+/* Device-side status bits of bounded waits that ran out since the last call
+ * (bit 0: the tensor-core tree build stopped on a wait), cleared on read.
+ * Waits for the device.  No counterpart in the reference. */
+int ftl_device_status(uint32_t *status_out);
 
 /* G_dst[node] = G_src[node] o mat (elementwise on the packed upper triangle);
  * mat_dev holds P FP64 values.  G_src may equal G_dst.
@@ -122,7 +157,7 @@ typedef struct ftl_krp_plan {
     void *eig_G;                         /* device, N x (2R-1) x P, prec */
     double *M;                           /* device workspace, (2N+3) x R x R FP64 */
     double *lambda;                      /* device workspace, (N+1) x R FP64 */
-    float *pinv32;                       /* device workspace, P FP32 (FP32 weights) */
+    float *pinv32;                       /* device workspace, one FP32 node (FP32 weights) */
     const float *U32[FTL_MAX_MODES];     /* optional, FP32 plans: FP32 copies of U (ftl_factor_shadow);
                                             leaf scans then read these rows; NULL: they read U */
 } ftl_krp_plan;

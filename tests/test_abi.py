@@ -44,10 +44,12 @@ def test_geometry_matches_oracle(n, F):
 def test_sizes():
     R = 32
     P = R * (R + 1) // 2
-    assert _lib.tree_bytes(2**23, 32, R, _lib.PREC["fp32"]) == (2 * 2**18 - 1) * P * 4
+    # FP32 nodes at 16 < R <= 32 use the wrapped-diagonal layout (544 values)
+    assert _lib.tree_bytes(2**23, 32, R, _lib.PREC["fp32"]) == (2 * 2**18 - 1) * 544 * 4
+    assert _lib.tree_bytes(2**10, 16, 16, _lib.PREC["fp32"]) == (2 * 2**6 - 1) * 136 * 4
     assert _lib.tree_bytes(1001, 8, 8, _lib.PREC["fp64"]) == (2 * 126 - 1) * 36 * 8
     e, m, l, p = _lib.plan_sizes(3, R, _lib.PREC["fp64"])
-    assert e == 3 * (2 * R - 1) * P * 8 and l == 4 * R * 8 and p == P * 4
+    assert e == 3 * (2 * R - 1) * P * 8 and l == 4 * R * 8 and p == 544 * 4  # pinv32: one FP32 node
     assert m >= 5 * R * R * 8
 
 
@@ -107,3 +109,28 @@ def test_sparse_and_als_handles_reject_bad_arguments_without_touching_the_device
     A = ctypes.c_void_p(9)
     assert L.ftl_als_create(None, 8, 100, 0, 1, ctypes.byref(A)) == 1
     assert L.ftl_sparse_destroy(None) == 0 and L.ftl_als_destroy(None) == 0
+
+
+@pytest.mark.parametrize("R,prec", [(8, "fp32"), (16, "fp32"), (17, "fp32"), (25, "fp32"), (32, "fp32"),
+                                    (33, "fp32"), (32, "fp64"), (5, "fp64"), (128, "fp32")])
+def test_node_layout_positions(R, prec):
+    """Every upper-triangle element has its own position inside the node
+    stride; the wrapped-diagonal layout (FP32, 16 < R <= 32) puts (a, b) at
+    diagonal (b - a) mod 32 of row a (or of row b past distance 16)."""
+    import numpy as np
+    lay, S, pos = _lib.node_layout(R, _lib.PREC[prec])
+    P = R * (R + 1) // 2
+    assert pos.shape == (P,) and len(set(pos.tolist())) == P and pos.min() >= 0 and pos.max() < S
+    assert S * (4 if prec == "fp32" else 8) % 16 == 0
+    if prec == "fp32" and 16 < R <= 32:
+        assert lay == 1 and S == 544
+        e = 0
+        for a in range(R):
+            for b in range(a, R):
+                d = (b - a) % 32
+                r, dd = (a, d) if d <= 16 else (b, 32 - d)
+                want = ((dd // 4) * 32 + r) * 4 + dd % 4 if dd < 16 else 512 + r
+                assert pos[e] == want
+                e += 1
+    else:
+        assert lay == 0 and np.array_equal(pos, np.arange(P))

@@ -23,7 +23,7 @@ def test_bad_shapes_raise():
     with pytest.raises(ValueError):
         ftl.Sampler([np.zeros((10, 200))], 10, 200, "efficient")
     with pytest.raises(ValueError):
-        ftl.Sampler([np.zeros((10, 4))], 10, 4, "efficient", precision="bf16")
+        ftl.Sampler([np.zeros((10, 4))], 10, 4, "efficient", precision="fp16")
 
 
 def test_output_arrays_are_checked_not_copied():
