@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--J", type=int, default=50000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="sampling",
-                    choices=["sampling", "als", "serve", "lowrank", "launcher-check"],
+                    choices=["sampling", "als", "serve", "lowrank", "tree", "launcher-check"],
                     help="als: randomized CP-ALS on the synthetic sparse tensor (seconds per sweep); "
                          "serve: Poisson stream of sampling and CP-ALS requests (p50/p99 latency)")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
@@ -577,6 +577,68 @@ def run_reference(args, ws, rank):
     }
 
 
+def tree_build_rates(U, R, precisions, reps=10):
+    """Device time of one partition-tree build (leaf Grams, the FP32 factor
+    copy for FP32-node trees, internal levels) per precision on the factor U,
+    and its HBM rate: bytes = read U (n R 8) + write the FP32 copy (n R 4) +
+    write the leaf level + read and write the internal levels (each internal
+    node is written once and read by its parent)."""
+    import torch
+    from fast_tensor_leverage_gb300 import _lib
+    n = U.shape[0]
+    F = min(R, n)
+    g = _lib.tree_geometry(n, F)
+    st = torch.cuda.current_stream(U.device)
+    peak, _ = measured_peak()
+    out = {}
+    for prec in precisions:
+        p = _lib.PREC[prec]
+        _, S, _ = _lib.node_layout(R, p)
+        es = 8 if prec == "fp64" else 4
+        G = torch.empty(_lib.tree_bytes(n, F, R, p) // es, dtype=torch.float64 if es == 8 else torch.float32,
+                        device=U.device)
+        U32 = torch.empty((n, R), dtype=torch.float32, device=U.device) if es == 4 else None
+
+        def build():
+            _lib.call("ftl_tree_build_ex", U.data_ptr(), n, R, F, p, G.data_ptr(),
+                      U32.data_ptr() if U32 is not None else None, st.cuda_stream)
+
+        for _ in range(3):
+            build()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            build()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        node_b = S * es
+        internal = g.node_count - g.leaf_count
+        byts = n * R * 8 + (n * R * 4 if es == 4 else 0) + g.leaf_count * node_b + 2 * internal * node_b
+        out[prec] = {"ms": ms, "GBps": byts / ms / 1e6, "frac_of_hbm": byts / ms / 1e6 / peak,
+                     "bytes": byts, "leaf_path": ("tensor cores (tcgen05)" if prec in ("tf32x3", "bf16") and R <= 32
+                                                  else "CUDA cores")}
+        del G, U32
+    out["device_status"] = _lib.device_status()
+    return out
+
+
+def run_tree(args, ws, rank, local):
+    """Partition-tree build throughput at the sampling workload's factor shape
+    (I = 2^log2I rows x R, N(0,1) with 1% of rows x100), per tree precision."""
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    I, R = 1 << args.log2I, args.R
+    U = make_factors_device(1, I, R, replica_seeds(rank)["factors"], dev)[0]
+    res = tree_build_rates(U, R, ("fp32", "tf32x3", "bf16", "fp64"), reps=max(3, args.steps))
+    if rank != 0:
+        return None
+    return {"metric": f"partition-tree build, I=2^{args.log2I}, R={R}", "unit": "ms", "value": res["fp32"]["ms"],
+            "higher_is_better": False, "n_gpus": ws, "builds": res,
+            "peak_hbm_gbs": measured_peak()[0], "data": "synthetic (seeded N(0,1), 1% rows x100)"}
+
+
 def run_als(args, ws, rank, local):
     """Randomized CP-ALS on the synthetic stand-in for amazon-reviews:
     dims 4.8e6 x 1.8e6 x 1.8e6, Zipf(1.1) indices, nnz unique tuples,
@@ -789,6 +851,11 @@ def main():
             return
         os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "expandable_segments:True")
         line = run_serve(args, ws, rank, local)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if args.workload == "tree":
+        line = run_tree(args, ws, rank, local)
         if line is not None:
             print(json.dumps(line), flush=True)
         return

@@ -50,8 +50,14 @@
 #ifndef FTL_DESC_RESIDENT_F64
 #define FTL_DESC_RESIDENT_F64 512
 #endif
+#ifndef FTL_DESC_CHAINS_D32
+#define FTL_DESC_CHAINS_D32 2      // FP32 DIAG32 draws: samples one warp descends in lockstep
+#endif
+#ifndef FTL_DESC_WARPS_D32
+#define FTL_DESC_WARPS_D32 4       // FP32 DIAG32 draws: warps per block
+#endif
 #ifndef FTL_DESC_RESIDENT_D32
-#define FTL_DESC_RESIDENT_D32 768  // FP32 DIAG32 kernels: 17 outer-product weights in registers (80 registers, no spills)
+#define FTL_DESC_RESIDENT_D32 640  // FP32 DIAG32 draws: threads per SM the register budget is set for
 #endif
 
 namespace ftl {
@@ -69,10 +75,12 @@ struct Shape {
 // 8256-entry packed outer product (33 KB in FP32, 66 KB in FP64) next to the
 // block's pair table (16.5 KB): 6 FP32 warps fit one block per SM (224 KB),
 // where blocks of 2 gave 2 blocks per SM (4 warps).
-template <int RMAX, typename T>
+template <int RMAX, typename T, bool DIAG = false>
 struct Blk {
     static constexpr int WARPS =
-        RMAX <= 64 ? Shape<RMAX>::WARPS : (sizeof(T) == 4 ? FTL_DESC_WARPS128_F32 : Shape<RMAX>::WARPS);
+        (DIAG && sizeof(T) == 4)
+            ? FTL_DESC_WARPS_D32
+            : (RMAX <= 64 ? Shape<RMAX>::WARPS : (sizeof(T) == 4 ? FTL_DESC_WARPS128_F32 : Shape<RMAX>::WARPS));
 };
 
 // 16-byte vector of the tree precision.
@@ -254,8 +262,10 @@ struct QFormD32 {
     float *s;  // unused (interface of QForm)
     int P, S;
 
-    __device__ __forceinline__ void setup(const float *x, const uint16_t *, int lane) {
-        const float xa = x[lane];
+    __device__ __forceinline__ void setup(const float *x, const uint16_t *, int lane) { setup_reg(x[lane], lane); }
+
+    // lane a passes x_a (zero for a >= R)
+    __device__ __forceinline__ void setup_reg(float xa, int lane) {
         xx[0] = xa * xa;
 #pragma unroll
         for (int d = 1; d < 16; ++d) xx[d] = (xa + xa) * __shfl_sync(0xffffffffu, xa, (lane + d) & 31);
@@ -264,26 +274,30 @@ struct QFormD32 {
 
     __device__ __forceinline__ float partial(const float *__restrict__ node, int lane) const {
         const float4 *v = reinterpret_cast<const float4 *>(node);
-        const float4 g0 = __ldg(v + lane), g1 = __ldg(v + 32 + lane), g2 = __ldg(v + 64 + lane),
-                     g3 = __ldg(v + 96 + lane);
-        const float g16 = __ldg(node + 512 + lane);
-        float acc = g0.x * xx[0];
-        acc = fmaf(g0.y, xx[1], acc);
-        acc = fmaf(g0.z, xx[2], acc);
-        acc = fmaf(g0.w, xx[3], acc);
-        acc = fmaf(g1.x, xx[4], acc);
-        acc = fmaf(g1.y, xx[5], acc);
-        acc = fmaf(g1.z, xx[6], acc);
-        acc = fmaf(g1.w, xx[7], acc);
-        acc = fmaf(g2.x, xx[8], acc);
-        acc = fmaf(g2.y, xx[9], acc);
-        acc = fmaf(g2.z, xx[10], acc);
-        acc = fmaf(g2.w, xx[11], acc);
-        acc = fmaf(g3.x, xx[12], acc);
-        acc = fmaf(g3.y, xx[13], acc);
-        acc = fmaf(g3.z, xx[14], acc);
-        acc = fmaf(g3.w, xx[15], acc);
-        return fmaf(g16, xx[16], acc);
+        const float4 g[4] = {__ldg(v + lane), __ldg(v + 32 + lane), __ldg(v + 64 + lane), __ldg(v + 96 + lane)};
+        return dot(g, __ldg(node + 512 + lane));
+    }
+
+    // this lane's part of the form from its row of a node (already loaded):
+    // two independent FMA chains (half the dependent latency)
+    __device__ __forceinline__ float dot(const float4 (&g)[4], float g16) const {
+        float a0 = g[0].x * xx[0], a1 = g[0].y * xx[1];
+        a0 = fmaf(g[0].z, xx[2], a0);
+        a1 = fmaf(g[0].w, xx[3], a1);
+        a0 = fmaf(g[1].x, xx[4], a0);
+        a1 = fmaf(g[1].y, xx[5], a1);
+        a0 = fmaf(g[1].z, xx[6], a0);
+        a1 = fmaf(g[1].w, xx[7], a1);
+        a0 = fmaf(g[2].x, xx[8], a0);
+        a1 = fmaf(g[2].y, xx[9], a1);
+        a0 = fmaf(g[2].z, xx[10], a0);
+        a1 = fmaf(g[2].w, xx[11], a1);
+        a0 = fmaf(g[3].x, xx[12], a0);
+        a1 = fmaf(g[3].y, xx[13], a1);
+        a0 = fmaf(g[3].z, xx[14], a0);
+        a1 = fmaf(g[3].w, xx[15], a1);
+        a0 = fmaf(g16, xx[16], a0);
+        return a0 + a1;
     }
 
     __device__ __forceinline__ float eval(const float *__restrict__ node, int lane) const {
@@ -423,14 +437,28 @@ __device__ __forceinline__ void df_sub(float &th, float &tl, float m) {
     th = nh;
 }
 
+// A uniform in [0, 1) as a double-float dh + dl (dh its FP32 rounding, dl
+// the FP32 rounding of the rest): exact to about 2^-48.
+__device__ __forceinline__ void split_df(double d, float &dh, float &dl) {
+    dh = d2f_rn(d);
+    dl = (float)(d - (double)dh);
+}
+
+// The same for a Philox uniform given by its 53 bits B (uniform = B 2^-53):
+// dh = (B >> 29) 2^-24 exactly, dl = the low 29 bits 2^-53 -- integer
+// conversions only.
+__device__ __forceinline__ void split_bits53(uint64_t B, float &dh, float &dl) {
+    dh = (float)(uint32_t)(B >> 29) * 5.9604644775390625e-08f;         // 2^-24
+    dl = (float)(uint32_t)(B & 0x1fffffffu) * 1.1102230246251565e-16f;  // 2^-53
+}
+
 template <int RMAX, class QF>
-__device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, const DGeom &g,
-                                           double draw, const QF &qf, int lane,
-                                           float &frac, const double *U = nullptr, int R = 0,
-                                           float *mroot = nullptr) {
+__device__ __forceinline__ int64_t descend_df(const float *__restrict__ G, int S, const DGeom &g, float dh,
+                                              float dl, const QF &qf, int lane, float &frac,
+                                              const double *U = nullptr, int R = 0, float *mroot = nullptr) {
     int64_t c = 0;
     if (is_leaf(g, 0)) {  // single-leaf tree: the leaf fraction is the draw
-        frac = (float)draw;
+        frac = fminf(dh + dl, 1.0f);
         if (mroot) *mroot = 1.0f;  // not evaluated; the leaf scan sees the block
         return 0;
     }
@@ -443,9 +471,14 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
         mL0 = qf.eval(G + S, lane);
     }
     if (mroot) *mroot = mP;
-    double t0 = draw * (double)mP;
-    float th = (float)t0;
-    float tl = (float)(t0 - (double)th);
+    // t = draw * mP in double-float (exact product of dh and mP, plus dl mP)
+    float th = dh * mP;
+    float tl = fmaf(dl, mP, fmaf(dh, mP, -th));
+    {
+        const float s = th + tl;
+        tl = tl - (s - th);
+        th = s;
+    }
     // 32-bit node index and level counter (node counts are far below 2^31:
     // a tree is at most 2 I / F nodes)
     const uint32_t ncount = (uint32_t)g.node_count;
@@ -474,6 +507,16 @@ __device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, c
     float f = mP > 0.0f ? (th + tl) / mP : 0.0f;
     frac = fminf(fmaxf(f, 0.0f), 1.0f);
     return c;
+}
+
+template <int RMAX, class QF>
+__device__ __forceinline__ int64_t descend(const float *__restrict__ G, int S, const DGeom &g,
+                                           double draw, const QF &qf, int lane,
+                                           float &frac, const double *U = nullptr, int R = 0,
+                                           float *mroot = nullptr) {
+    float dh, dl;
+    split_df(draw, dh, dl);
+    return descend_df<RMAX, QF>(G, S, g, dh, dl, qf, lane, frac, U, R, mroot);
 }
 
 // The FP32 descent above carries the mass of a right child as parent - left
@@ -521,6 +564,110 @@ __device__ __forceinline__ int64_t descend_careful(const float *__restrict__ G, 
     }
     frac = m > 0.0 ? (float)fmin(fmax(t / m, 0.0), 1.0) : 0.0f;
     return c;
+}
+
+// Lockstep descents of NC independent queries through one DIAG32 FP32 tree
+// (one warp, lane a = row a): each level issues every chain's node loads
+// before any form is computed, so NC dependent read chains are in flight at
+// once; the root and its left child, common to all chains, are read once.
+// The decisions are descend_df's: t = draw * m_root in double-float, left
+// iff t <= m_left, a right turn subtracts m_left.  cu[c] receives the leaf,
+// frac[c] the leaf fraction, mroot[c] the root form.
+template <int NC>
+__device__ __forceinline__ void descend_d32_multi(const float *__restrict__ G, const DGeom &g, const float (&dh)[NC],
+                                                  const float (&dl)[NC], const QFormD32 (&qf)[NC], int lane,
+                                                  uint32_t (&cu)[NC], float (&frac)[NC], float (&mroot)[NC]) {
+    constexpr int S = kDiag32Stride;
+    if (is_leaf(g, 0)) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            cu[c] = 0;
+            frac[c] = fminf(dh[c] + dl[c], 1.0f);
+            mroot[c] = 1.0f;
+        }
+        return;
+    }
+    float th[NC], tl[NC], mP[NC], mL[NC];
+    {
+        const float4 *r4 = reinterpret_cast<const float4 *>(G), *l4 = reinterpret_cast<const float4 *>(G + S);
+        const float4 rv[4] = {__ldg(r4 + lane), __ldg(r4 + 32 + lane), __ldg(r4 + 64 + lane), __ldg(r4 + 96 + lane)};
+        const float4 lv[4] = {__ldg(l4 + lane), __ldg(l4 + 32 + lane), __ldg(l4 + 64 + lane), __ldg(l4 + 96 + lane)};
+        const float r16 = __ldg(G + 512 + lane), l16 = __ldg(G + S + 512 + lane);
+        float a[NC], b[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            a[c] = qf[c].dot(rv, r16);
+            b[c] = qf[c].dot(lv, l16);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                a[c] += __shfl_xor_sync(0xffffffffu, a[c], o);
+                b[c] += __shfl_xor_sync(0xffffffffu, b[c], o);
+            }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            mroot[c] = mP[c] = a[c];
+            mL[c] = b[c];
+            th[c] = dh[c] * mP[c];
+            tl[c] = fmaf(dl[c], mP[c], fmaf(dh[c], mP[c], -th[c]));
+            const float s = th[c] + tl[c];
+            tl[c] = tl[c] - (s - th[c]);
+            th[c] = s;
+            cu[c] = 0;
+        }
+    }
+    const uint32_t ncount = (uint32_t)g.node_count;
+    const int lf = (int)g.lfill_level;
+    for (int lvl = 0; lvl <= lf; ++lvl) {
+        bool go[NC];
+        bool any = false;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            go[c] = !(lvl == lf && 2u * cu[c] + 1u >= ncount);
+            any |= go[c];
+        }
+        if (!any) break;
+        if (lvl > 0) {
+            float4 v[NC][4];
+            float v16[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const float *node = G + (size_t)(go[c] ? 2u * cu[c] + 1u : 0u) * (size_t)S;
+                const float4 *n4 = reinterpret_cast<const float4 *>(node);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) v[c][q] = __ldg(n4 + 32 * q + lane);
+                v16[c] = __ldg(node + 512 + lane);
+            }
+            float part[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) part[c] = qf[c].dot(v[c], v16[c]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) part[c] += __shfl_xor_sync(0xffffffffu, part[c], o);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) mL[c] = part[c];
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            if (!go[c]) continue;
+            if (((th[c] - mL[c]) + tl[c]) <= 0.0f) {
+                cu[c] = 2u * cu[c] + 1u;
+                mP[c] = mL[c];
+            } else {
+                cu[c] = 2u * cu[c] + 2u;
+                df_sub(th[c], tl[c], mL[c]);
+                mP[c] = fmaxf(mP[c] - mL[c], 0.0f);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const float f = mP[c] > 0.0f ? (th[c] + tl[c]) / mP[c] : 0.0f;
+        frac[c] = fminf(fmaxf(f, 0.0f), 1.0f);
+    }
 }
 
 // ------------------------------------------------------------- leaf scan
@@ -697,6 +844,91 @@ __device__ __forceinline__ int64_t leaf_scan(const UT *__restrict__ U, int R, co
     }
     if (res >= rows) res = rows - 1;
     return row0 + res;
+}
+
+// Leaf row selection for R = F = 32 from the FP32 factor copy (the same
+// rule as leaf_scan's FP32 branch): the 32 x 32 block is read as eight
+// 512-byte warp loads of 16-byte vectors (lane l, step t: row 4t + l/8,
+// columns 4(l%8)..+3), each lane forms four-column partial dot products
+// with the query xa (lane a holds x_a), a three-step transpose-reduce
+// within groups of eight lanes leaves row 4(l%8) + l/8's form in lane l, a
+// shuffle puts row r's square in lane r, and a warp inclusive scan gives the
+// prefix.  Rows past a partial last block read as zero and are never chosen.
+__device__ __forceinline__ int64_t leaf_scan_d32(const float *__restrict__ U32, const DGeom &g, int64_t c,
+                                                 float frac, float xa, int lane, bool &empty) {
+    const int64_t leaf = leaf_index(g, c);
+    const int64_t row0 = leaf * 32;
+    const int rows = (int)min((int64_t)32, g.n - row0);
+    const float4 *blk = reinterpret_cast<const float4 *>(U32 + row0 * 32);
+    const int cg = lane & 7, rg = lane >> 3;
+    float xq[4];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) xq[w] = __shfl_sync(0xffffffffu, xa, 4 * cg + w);
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (4 * t + rg < rows) u = __ldg(blk + 32 * t + lane);
+        v[t] = fmaf(u.w, xq[3], fmaf(u.z, xq[2], fmaf(u.y, xq[1], u.x * xq[0])));
+    }
+    // transpose-reduce over the 8 lanes of a group (offsets 4, 2, 1)
+#pragma unroll
+    for (int off = 4, live = 8; off >= 1; off >>= 1, live >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (i < live / 2) {
+                const float send = upper ? v[i] : v[i + live / 2];
+                const float keep = upper ? v[i + live / 2] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+            }
+        }
+    }
+    const float q = v[0];  // form of row 4 cg + rg
+    float q2 = __shfl_sync(0xffffffffu, q * q, 8 * (lane & 3) + (lane >> 2));  // row `lane`
+    if (lane >= rows) q2 = 0.0f;
+    float incl = q2;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    const float tot = __shfl_sync(0xffffffffu, incl, 31);
+    const unsigned bal = __ballot_sync(0xffffffffu, lane <= 30 && frac * tot < incl);
+    int res = 31;
+    empty = false;
+    if (bal) {
+        res = __ffs(bal) - 1;
+    } else {
+        // the last row with a positive form, or an all-zero block (redone)
+        const unsigned pos = __ballot_sync(0xffffffffu, q2 > 0.0f);
+        if (pos) res = 31 - __clz((int)pos);
+        else empty = true;
+    }
+    if (res >= rows) res = rows - 1;
+    return row0 + res;
+}
+
+// x * 2^sh rounded to FP32 by integer operations (x * 2^sh below 2^-126 is
+// flushed to zero; the caller's shift keeps the largest |x| in [1, 2)).
+__device__ __forceinline__ float scaled_f32(double x, int sh) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const int es = e + sh;
+    if (e == 0 || es < 897) return __uint_as_float(hi & 0x80000000u);
+    unsigned r = ((unsigned)(es - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;
+    return __uint_as_float((hi & 0x80000000u) | r);
+}
+
+// The shift that puts the largest |x| of the warp's vector (lane a holds x_a,
+// zero past R) in [1, 2): 1023 - (largest biased FP64 exponent).
+__device__ __forceinline__ int query_shift(double x) {
+    const int e = (int)(((unsigned)__double2hiint(x) >> 20) & 0x7ffu);
+    const int emax = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+    return (emax >= 1 && emax <= 2045) ? 1023 - emax : 0;
 }
 
 // Packed (a << 8 | b) table of the upper triangle in row-major order.

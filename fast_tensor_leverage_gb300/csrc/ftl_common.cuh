@@ -222,7 +222,8 @@ __host__ __device__ inline void philox_round(uint32_t c[4], uint32_t k[2]) {
     c[3] = lo0;
 }
 
-__host__ __device__ inline double philox_uniform(uint64_t seed, uint64_t counter) {
+// The 53 random bits of uniform #counter: the uniform is bits * 2^-53.
+__host__ __device__ inline uint64_t philox_bits53(uint64_t seed, uint64_t counter) {
     uint32_t c[4] = {(uint32_t)counter, (uint32_t)(counter >> 32), 0u, 0u};
     uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
@@ -232,8 +233,11 @@ __host__ __device__ inline double philox_uniform(uint64_t seed, uint64_t counter
         k[0] += W0;
         k[1] += W1;
     }
-    uint64_t bits = ((uint64_t)(c[0] >> 5) << 26) | (uint64_t)(c[1] >> 6);
-    return (double)bits * (1.0 / 9007199254740992.0);  // 2^-53
+    return ((uint64_t)(c[0] >> 5) << 26) | (uint64_t)(c[1] >> 6);
+}
+
+__host__ __device__ inline double philox_uniform(uint64_t seed, uint64_t counter) {
+    return (double)philox_bits53(seed, counter) * (1.0 / 9007199254740992.0);  // 2^-53
 }
 
 }  // namespace ftl

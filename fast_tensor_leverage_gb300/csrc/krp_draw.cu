@@ -183,15 +183,122 @@ struct Resident {
         sizeof(T) == 8 ? FTL_DESC_RESIDENT_F64 : (DIAG ? FTL_DESC_RESIDENT_D32 : FTL_DESC_RESIDENT_F32);
 };
 
+// Samples i0 + c (c < NC, those below J) of one draw for FP32 trees in the
+// DIAG32 layout (16 < R <= 32): the descents of draw_sample with registers
+// only, the NC samples' descents in lockstep (descend_d32_multi) so that
+// their dependent node reads overlap.  Lane l < 2N draws uniform l of each
+// sample (phase l / N, mode l % N: the reference's 2N x J layout) once, as
+// an FP32 pair; the queries are the FP64 vectors h and h o W[u] scaled by a
+// power of two and rounded to FP32 with integer operations; lane a keeps
+// x_a, its 17 outer-product weights and h_a; R = F = 32 leaf blocks are
+// scanned with vector loads from the FP32 factor copy.  FP64 work per mode:
+// h o W[u] and the h update.  Samples that meet a zero-mass block are
+// flagged for the careful redo as in draw_sample.  Each sample's arithmetic
+// does not depend on NC.
+template <bool S32, int NC>
+__device__ __forceinline__ void draw_samples_d32(const DrawParams &p, int64_t i0, int lane) {
+    const int R = p.R, N = p.N;
+    const size_t RR = (size_t)R * R;
+    const float RJ = (float)((double)R / (double)p.J);
+    const bool col = lane < R;
+    float uh[NC], ul[NC];
+    double h[NC];
+    QFormD32 qf[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        uh[c] = ul[c] = 0.0f;
+        const int64_t i = i0 + c;
+        if (lane < 2 * N && i < p.J) {
+            const int64_t idx = (int64_t)lane * p.J + i;
+            if (p.draws)
+                split_df(p.draws[idx], uh[c], ul[c]);
+            else
+                split_bits53(philox_bits53(p.seed, p.ctr + (uint64_t)idx), uh[c], ul[c]);
+        }
+        h[c] = col ? 1.0 : 0.0;
+    }
+#pragma unroll 1
+    for (int k = 0; k < N; ++k) {
+        if ((uint32_t)k == p.j) continue;
+        float dh[NC], dl[NC], frac[NC], mroot[NC], xf[NC];
+        uint32_t cu[NC];
+        // eigen-component descents, query h
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            qf[c].setup_reg(scaled_f32(h[c], query_shift(h[c])), lane);
+            dh[c] = __shfl_sync(0xffffffffu, uh[c], k);
+            dl[c] = __shfl_sync(0xffffffffu, ul[c], k);
+        }
+        const float *Ge = (const float *)p.eig_G + (size_t)k * (size_t)(2 * R - 1) * kDiag32Stride;
+        descend_d32_multi<NC>(Ge, p.eig, dh, dl, qf, lane, cu, frac, mroot);
+        // Gram-tree descents, query h o W[u]
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const double *Wr = p.M + (size_t)p.offset[k] * RR + (size_t)leaf_index(p.eig, cu[c]) * R;
+            const double x = col ? h[c] * Wr[lane] : 0.0;
+            xf[c] = scaled_f32(x, query_shift(x));
+            qf[c].setup_reg(xf[c], lane);
+            dh[c] = __shfl_sync(0xffffffffu, uh[c], N + k);
+            dl[c] = __shfl_sync(0xffffffffu, ul[c], N + k);
+        }
+        const DGeom &g = p.gram[k];
+        descend_d32_multi<NC>((const float *)p.gram_G[k], g, dh, dl, qf, lane, cu, frac, mroot);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            bool empty = false;
+            int64_t t;
+            if (FTL_DESC_REDO && !(mroot[c] > 0.0f)) {
+                empty = true;  // zero query: the eigen component has no mass under h
+                t = leaf_index(g, cu[c]) * g.F;
+            } else if (g.F > 1) {
+                if (S32 && R == 32 && g.F == 32) {
+                    t = leaf_scan_d32(p.U32[k], g, cu[c], frac[c], xf[c], lane, empty);
+                } else {
+                    LaneQuery<32, float> lq;
+                    lq.v[0] = xf[c];
+                    t = S32 ? leaf_scan<32, float, float>(p.U32[k], R, g, cu[c], frac[c], lq, lane, empty)
+                            : leaf_scan<32, float, double>(p.U[k], R, g, cu[c], frac[c], lq, lane, empty);
+                }
+            } else {
+                t = leaf_index(g, cu[c]);
+            }
+            if (!FTL_DESC_REDO) empty = false;
+            if (col) h[c] *= p.U[k][t * R + lane];
+            if (lane == 0 && i0 + c < p.J) p.samples[(int64_t)k * p.J + i0 + c] = empty ? kRedoSample : (uint64_t)t;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const int64_t i = i0 + c;
+        if (p.weights) {
+            // w = R / (J lev), lev = h^T pinv h = lev_s 2^(-2 sh)
+            const int sh = query_shift(h[c]);
+            qf[c].setup_reg(scaled_f32(h[c], sh), lane);
+            const float lev_s = qf[c].eval(p.pinv32, lane);
+            if (lane == 0 && i < p.J) {
+                const double sc = (sh >= -1022 && sh <= 1023) ? __hiloint2double((1023 + sh) << 20, 0) : 0.0;
+                p.weights[i] = (double)(RJ / lev_s) * sc * sc;
+            }
+        }
+        if (p.h && col && i < p.J) p.h[i * R + lane] = h[c];
+    }
+}
+
 template <int RMAX, typename T, bool S32, bool DIAG>
-__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    DrawWarp<RMAX, T, DIAG> dw;
-    setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, p.R, p.P, p.S);
+__global__ void __launch_bounds__(Blk<RMAX, T, DIAG>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T, DIAG>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
+    constexpr int WARPS = Blk<RMAX, T, DIAG>::WARPS;
     const int warp = threadIdx.x >> 5;
-    for (int64_t i = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; i < p.J;
-         i += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS)
-        draw_sample<RMAX, T, false, S32, DIAG>(p, i, dw);
+    if constexpr (DIAG && sizeof(T) == 4) {
+        constexpr int NC = FTL_DESC_CHAINS_D32;
+        for (int64_t i0 = ((int64_t)blockIdx.x * WARPS + warp) * NC; i0 < p.J; i0 += (int64_t)gridDim.x * WARPS * NC)
+            draw_samples_d32<S32, NC>(p, i0, threadIdx.x & 31);
+    } else {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        DrawWarp<RMAX, T, DIAG> dw;
+        setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, p.R, p.P, p.S);
+        for (int64_t i = (int64_t)blockIdx.x * WARPS + warp; i < p.J; i += (int64_t)gridDim.x * WARPS)
+            draw_sample<RMAX, T, false, S32, DIAG>(p, i, dw);
+    }
 }
 
 // Packed draw: the samples of up to FTL_MAX_PACK requests of the same rank
@@ -205,17 +312,28 @@ struct MultiDrawParams {
 };
 
 template <int RMAX, typename T, bool S32, bool DIAG>
-__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    DrawWarp<RMAX, T, DIAG> dw;
-    setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+__global__ void __launch_bounds__(Blk<RMAX, T, DIAG>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T, DIAG>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
+    constexpr int WARPS = Blk<RMAX, T, DIAG>::WARPS;
     const int warp = threadIdx.x >> 5;
     const int64_t total = mp.cum[mp.n];
-    for (int64_t g = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; g < total;
-         g += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS) {
-        int r = 0;
-        while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
-        draw_sample<RMAX, T, false, S32, DIAG>(mp.req[r], g - mp.cum[r], dw);
+    if constexpr (DIAG && sizeof(T) == 4) {
+        // one sample per warp (neighbouring samples may belong to different
+        // requests, i.e. different trees); the same per-sample arithmetic as
+        // krp_draw_kernel
+        for (int64_t g = (int64_t)blockIdx.x * WARPS + warp; g < total; g += (int64_t)gridDim.x * WARPS) {
+            int r = 0;
+            while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
+            draw_samples_d32<S32, 1>(mp.req[r], g - mp.cum[r], threadIdx.x & 31);
+        }
+    } else {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        DrawWarp<RMAX, T, DIAG> dw;
+        setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+        for (int64_t g = (int64_t)blockIdx.x * WARPS + warp; g < total; g += (int64_t)gridDim.x * WARPS) {
+            int r = 0;
+            while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
+            draw_sample<RMAX, T, false, S32, DIAG>(mp.req[r], g - mp.cum[r], dw);
+        }
     }
 }
 
@@ -360,17 +478,28 @@ static size_t desc_smem() {
            (size_t)Blk<RMAX, T>::WARPS * WarpSlot<RMAX, T, DIAG>::bytes;
 }
 
+// The fast FP32 DIAG32 draw kernels use registers only (no dynamic shared
+// memory) and their own block shape; the fix-up kernels run the generic path.
+template <int RMAX, typename T, bool DIAG>
+struct FastD32 {
+    static constexpr bool value = DIAG && sizeof(T) == 4;
+};
+
 template <int RMAX, typename T, bool S32, bool DIAG>
 static int launch_draw(const DrawParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T, DIAG>();
     {
-        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32, DIAG>, smem, "krp_draw_kernel");
+        constexpr bool fast = FastD32<RMAX, T, DIAG>::value;
+        const int dwarps = Blk<RMAX, T, DIAG>::WARPS;
+        const int per_warp = fast ? FTL_DESC_CHAINS_D32 : 1;
+        const size_t dsmem = fast ? 0 : smem;
+        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32, DIAG>, dsmem, "krp_draw_kernel");
         if (arc) return arc;
+        int64_t blocks = (p.J + (int64_t)dwarps * per_warp - 1) / ((int64_t)dwarps * per_warp);
+        blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
+        krp_draw_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, dwarps * 32, dsmem, st>>>(p);
     }
-    int64_t blocks = (p.J + warps - 1) / warps;
-    blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     int rc = check_launch("krp_draw_kernel");
     if (rc || sizeof(T) == 8) return rc;
     {
@@ -387,14 +516,18 @@ template <int RMAX, typename T, bool S32, bool DIAG>
 static int launch_multi(const MultiDrawParams &mp, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T, DIAG>();
-    {
-        const int arc = ensure_smem((const void *)krp_draw_multi_kernel<RMAX, T, S32, DIAG>, smem, "krp_draw_multi_kernel");
-        if (arc) return arc;
-    }
     const int64_t total = mp.cum[mp.n];
-    int64_t blocks = (total + warps - 1) / warps;
-    blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_multi_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, warps * 32, smem, st>>>(mp);
+    {
+        constexpr bool fast = FastD32<RMAX, T, DIAG>::value;
+        const int dwarps = Blk<RMAX, T, DIAG>::WARPS;
+        const size_t dsmem = fast ? 0 : smem;
+        const int arc =
+            ensure_smem((const void *)krp_draw_multi_kernel<RMAX, T, S32, DIAG>, dsmem, "krp_draw_multi_kernel");
+        if (arc) return arc;
+        int64_t blocks = (total + dwarps - 1) / dwarps;
+        blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
+        krp_draw_multi_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, dwarps * 32, dsmem, st>>>(mp);
+    }
     int rc = check_launch("krp_draw_multi_kernel");
     if (rc || sizeof(T) == 8) return rc;
     {

@@ -3,14 +3,15 @@
 //
 // PartitionTree::build_tree (cpp_ext/partition_tree.hpp:120-170) forms
 // G_leaf = U_blk^T U_blk for every leaf block (dsyrk) and sums children up
-// the tree.  Here the leaf level runs as a persistent kernel, one CTA of four
-// warps per SM:
+// the tree.  Here the leaf level runs as a persistent kernel, one CTA of 16
+// warps per SM (the conversion is bound by instruction latency):
 //
 //   * TMA brings tiles of four consecutive leaf blocks (4F rows x R FP64
 //     values, contiguous in U) into a four-stage shared-memory ring
 //     (cp.async.bulk.tensor over a 2-D tensor map of U when R is even, the
 //     untiled cp.async.bulk otherwise), completion tracked by mbarriers.
-//   * Warp w converts leaf w of the tile: lane c takes column c, rounds the
+//   * Warps w, w+4, w+8, w+12 convert leaf w of the tile (8 of its 32 rows
+//     each): lane c takes column c, rounds the
 //     FP64 values to FP32 with integer operations (no FP64 instruction), and
 //     writes them as the K-major operand X^T (M = 128 rows: 32 columns of
 //     each of the four leaves; K = 32: the leaf's rows, zero padded) in the
@@ -44,7 +45,7 @@ __device__ unsigned int g_device_status;  // bit 0: a bounded wait of the tensor
 
 namespace tc {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 512;
 constexpr int kStages = 4;
 constexpr int kStageBytes = 128 * 32 * 8;   // 4 leaves x 32 rows x 32 FP64 columns
 constexpr int kOpBytes = 128 * 128;         // 128 operand rows x 128 bytes
@@ -275,10 +276,12 @@ __global__ void __launch_bounds__(kThreads, 1) leaf_gram_tc_kernel(const __grid_
     if (tid == 0)
         for (int64_t i = 0; i < min((int64_t)(kStages), (int64_t)(ntl)); ++i) issue_load(i);
 
-    // Epilogue of local tile i: warp w writes leaf w's node from accumulator
-    // i % 2.  The TMEM load is warp-collective: a warp whose wait failed in
-    // any lane skips it as a whole.
+    // Epilogue of local tile i: warp w < 4 writes leaf w's node from
+    // accumulator i % 2 (warp w reads TMEM lanes 32w..32w+31).  The TMEM load
+    // is warp-collective: a warp whose wait failed in any lane skips it as a
+    // whole.
     auto epilogue = [&](int64_t i) -> bool {
+        if (warp >= 4) return true;
         const int b = (int)(i & 1);
         const bool waited = mbar_wait(mmad + b, (uint32_t)((i >> 1) & 1), abort_flag);
         if (!__all_sync(0xffffffffu, waited)) return false;
@@ -286,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, 1) leaf_gram_tc_kernel(const __grid_
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * 128 + 32 * warp), v);
         tc_fence_before();
-        const int64_t leaf = (blockIdx.x + i * (int64_t)gridDim.x) * 4 + warp;
+        const int64_t leaf = (blockIdx.x + i * (int64_t)gridDim.x) * 4 + warp;  // warp < 4
         if (leaf < p.leaf_count) {
             float *xp = (float *)(smem + kOffXpose) + warp * 32 * 33;
 #pragma unroll
@@ -326,31 +329,32 @@ __global__ void __launch_bounds__(kThreads, 1) leaf_gram_tc_kernel(const __grid_
         const int s = (int)(i % kStages);
         const int b = (int)(i & 1);
         const bool waited = mbar_wait(full + s, (uint32_t)((i / kStages) & 1), abort_flag);
-        // convert: warp w = leaf w of the tile, lane = column
+        // convert: warp w = leaf w % 4 of the tile, rows 8 (w / 4) .. +7, lane = column
         if (waited) {
+            const int lw = warp & 3, kg = warp >> 2;
             const int64_t tile = blockIdx.x + i * (int64_t)gridDim.x;
             const int64_t row0 = tile * tile_rows;
-            const int64_t leaf = tile * 4 + warp;
+            const int64_t leaf = tile * 4 + lw;
             const int rows_leaf = leaf < p.leaf_count ? (int)min((int64_t)F, p.n - leaf * F) : 0;
             const double *st = (const double *)(smem + kOffStage + s * kStageBytes);
             const uint32_t copied = p.use_tmap ? 0xffffffffu : bulk_bytes(i);
             const int c = lane;
-            const int m = 32 * warp + c;
+            const int m = 32 * lw + c;
             unsigned char *op_hi = smem + kOffOp + (b * 2 + 0) * kOpBytes;
             unsigned char *op_lo = smem + kOffOp + (b * 2 + 1) * kOpBytes;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
+            for (int q = 2 * kg; q < 2 * kg + 2; ++q) {
                 float v[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int k = 4 * q + j;
                     double x = 0.0;
                     if (c < R && k < rows_leaf) {
-                        const int e = (warp * F + k) * R + c;  // element of the staged tile
+                        const int e = (lw * F + k) * R + c;  // element of the staged tile
                         x = ((uint32_t)e * 8u + 8u <= copied) ? st[e] : p.U[row0 * R + e];
                     }
                     v[j] = d2f_rn(x);
-                    if (p.U32 && c < R && k < rows_leaf) p.U32[row0 * R + (warp * F + k) * R + c] = v[j];
+                    if (p.U32 && c < R && k < rows_leaf) p.U32[row0 * R + (lw * F + k) * R + c] = v[j];
                 }
                 if (MODE == 0) {
                     float4 h, l;

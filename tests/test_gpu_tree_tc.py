@@ -4,8 +4,9 @@ three products, FP32 accumulation) and bf16 (BF16-rounded factor, FP32
 accumulation) -- against the FP64 Grams of the same factor.
 
 Tolerances (entrywise, relative to sqrt(G_aa G_bb) of the FP64 node):
-  * tf32x3: 2e-6 -- each product carries about 2^-21 relative error and the
-    FP32 sums over 32 rows and up to 20 levels about 1e-6;
+  * tf32x3 (and the FP32 CUDA-core build): 6e-6 -- each product carries
+    about 2^-21 relative error, and the FP32 sums over a leaf's 32 rows and
+    up to 20 levels above it add about 50 roundings of 2^-24 on a root path;
   * bf16: 1.6e-2 -- each factor entry is rounded to 8 significant bits.
 The FP32 copy of the factor written by the same pass equals the factor
 rounded to nearest FP32 exactly, and no bounded device wait ran out."""
@@ -15,7 +16,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"tf32x3": 2e-6, "bf16": 1.6e-2, "fp32": 2e-6}
+TOL = {"tf32x3": 6e-6, "bf16": 1.6e-2, "fp32": 6e-6}
 
 
 @pytest.fixture(scope="module")
