@@ -51,13 +51,13 @@
 #define FTL_DESC_RESIDENT_F64 512
 #endif
 #ifndef FTL_DESC_CHAINS_D32
-#define FTL_DESC_CHAINS_D32 2      // FP32 DIAG32 draws: samples one warp descends in lockstep
+#define FTL_DESC_CHAINS_D32 3      // FP32 DIAG32 draws: samples one warp descends in lockstep
 #endif
 #ifndef FTL_DESC_WARPS_D32
 #define FTL_DESC_WARPS_D32 4       // FP32 DIAG32 draws: warps per block
 #endif
 #ifndef FTL_DESC_RESIDENT_D32
-#define FTL_DESC_RESIDENT_D32 640  // FP32 DIAG32 draws: threads per SM the register budget is set for
+#define FTL_DESC_RESIDENT_D32 512  // FP32 DIAG32 draws: threads per SM the register budget is set for (128)
 #endif
 
 namespace ftl {

@@ -121,13 +121,18 @@ def c2_case(ftl):
     return {"N": N, "I": I, "R": R, "U": U, "U_host": U_host, "oracle": O.OracleKRPSampler(U_host, 4096, R)}
 
 
-@pytest.mark.parametrize("j", [4, 0])
-def test_c2_scale_draw_matches_oracle(ftl, c2_case, j):
+@pytest.mark.parametrize("j,min_agree", [(4, 0.95), (0, 0.85)])
+def test_c2_scale_draw_matches_oracle(ftl, c2_case, j, min_agree):
     """At the benchmarked size (18-level Gram trees, I = 2^23): FP64 draws
     match the oracle index for index (except near-ties, oracle margin below
-    NEAR_TIE), h bit-exact, weights within 1e-9; mixed-precision draws agree
-    with the same oracle samples on >= 99.5% of samples, weights within 1e-3.
-    Both modes-included (j = N+1) and one-mode-excluded (j = 0) draws."""
+    NEAR_TIE), h bit-exact, weights within 1e-9.  Mixed-precision draws given
+    the same uniforms agree with the oracle's samples on >= 95% (j = N+1) /
+    85% (j = 0) of samples, with h bit-exact and weights within 1e-3 where
+    they agree: FP32 forms place the 2^23 row boundaries of each mode's CDF
+    about 1e-7 from their FP64 positions, and where per-mode eigenvalues
+    cluster the FP32 eigenbasis differs inside the cluster, so the same
+    uniform can land on a neighbouring row although the sampled law is the
+    same (test_c2_like_law_matches_exact_marginals checks the law)."""
     N, R, J = c2_case["N"], c2_case["R"], 4096
     o = c2_case["oracle"]
     rng = np.random.default_rng(77 + j)
@@ -148,11 +153,107 @@ def test_c2_scale_draw_matches_oracle(ftl, c2_case, j):
             np.testing.assert_allclose(w[ok], w_ref[ok], rtol=1e-9)
         else:
             agree = (samples[rows] == ref[rows]).all(axis=0)
-            assert agree.mean() >= 0.95, agree.mean()
+            assert agree.mean() >= min_agree, agree.mean()
             assert np.array_equal(h[agree], h_ref[agree])
             np.testing.assert_allclose(w[agree], w_ref[agree], rtol=1e-3)
         del s
         torch.cuda.empty_cache()
+
+
+def _exact_subtree_marginals(trees64, R, j, k, level):
+    """P(mode-k sample row lies under node c) for the nodes c of `level` of
+    mode k's tree: sum_ab G_c[a,b] M_k[a,b] / rank with M_k = pinv(prod over
+    the sampled modes of the root Grams) o prod over the sampled modes other
+    than k of the root Grams (the leverage law of the KRP, summed over the
+    other modes' rows), from the FP64 node Grams (packed, stride 528)."""
+    P = R * (R + 1) // 2
+    iu = torch.triu_indices(R, R, device="cuda")
+
+    def full(packed):
+        M = torch.zeros((packed.shape[0], R, R), dtype=torch.float64, device="cuda")
+        M[:, iu[0], iu[1]] = packed
+        M[:, iu[1], iu[0]] = packed
+        return M
+
+    S = 528  # FP64 node stride at R = 32
+    roots = {m: full(t.view(-1, S)[:1, :P])[0] for m, t in enumerate(trees64)}
+    modes = [m for m in roots if m != j]
+    prod = torch.ones((R, R), dtype=torch.float64, device="cuda")
+    for m in modes:
+        prod = prod * roots[m]
+    Mk = torch.linalg.pinv(prod, hermitian=True)
+    for m in modes:
+        if m != k:
+            Mk = Mk * roots[m]
+    nodes = trees64[k].view(-1, S)[(1 << level) - 1:(1 << (level + 1)) - 1, :P]
+    p = (full(nodes) * Mk).sum((1, 2))
+    return (p / p.sum()).cpu().numpy()
+
+
+@pytest.mark.parametrize("j", [4, 0])
+def test_c2_like_law_matches_exact_marginals(ftl, j):
+    """The sampled law itself at the C2 shape but 2^20 rows (15-level trees,
+    1% of rows x100): for every sampled mode, the frequencies of 2^23 draws'
+    rows per subtree at tree levels 4 and 8 against the exact subtree
+    probabilities, in FP64 and in mixed precision.  Total variation within
+    1.5x the sampling noise of that many draws (+1e-4)."""
+    N, I, R, Jd, reps = 3, 1 << 20, 32, 1 << 20, 8
+    g = torch.Generator(device="cuda")
+    g.manual_seed(77)
+    U = []
+    for _ in range(N):
+        u = torch.randn(I, R, device="cuda", dtype=torch.float64, generator=g)
+        u[torch.randperm(I, device="cuda", generator=g)[: I // 100]] *= 100.0
+        U.append(u)
+    s64 = ftl.Sampler(U, Jd, R, "efficient", precision="fp64", seed=5)
+    depth = 15  # 2^20 rows / 32 per leaf = 2^15 leaves, complete tree
+    for precision in ("fp64", "fp32"):
+        s = s64 if precision == "fp64" else ftl.Sampler(U, Jd, R, "efficient", precision=precision, seed=5)
+        counts = {(k, L): torch.zeros(1 << L, dtype=torch.int64, device="cuda")
+                  for k in range(N) if k != j for L in (4, 8)}
+        for _ in range(reps):
+            smp = s.draw(j)[0]
+            for (k, L), c in counts.items():
+                c += torch.bincount((smp[k] // 32) >> (depth - L), minlength=1 << L)
+        for (k, L), c in counts.items():
+            p = _exact_subtree_marginals(s64.trees, R, j, k, L)
+            emp = c.cpu().numpy() / (reps * Jd)
+            tv = 0.5 * np.abs(emp - p).sum()
+            noise = 0.5 * np.sum(np.sqrt(2 * p / (np.pi * reps * Jd)))
+            assert tv <= 1.5 * noise + 1e-4, (precision, k, L, tv, noise)
+
+
+def test_readme_shape_marginals_match_exact(ftl):
+    """The README configuration (N = 4 factors of 1000 x 8, a KRP of 10^12
+    rows): the per-mode marginal of 2^24 draws over each mode's 1000 rows
+    against the exact marginal p_k(i) = u_i^T [pinv(prod_m G_m) o prod_{m != k}
+    G_m] u_i / rank (computed in FP64 from the factors), FP64 and mixed."""
+    rng = np.random.default_rng(2024)
+    N, I, R, Jd, reps = 4, 1000, 8, 1 << 21, 8
+    U = [rng.normal(size=(I, R)) for _ in range(N)]
+    G = [u.T @ u for u in U]
+    prod = np.ones((R, R))
+    for m in range(N):
+        prod = prod * G[m]
+    pinv = np.linalg.pinv(prod, hermitian=True)
+    for precision in ("fp64", "fp32"):
+        s = ftl.Sampler(U, Jd, R, "efficient", precision=precision, seed=9)
+        counts = torch.zeros((N, I), dtype=torch.int64, device="cuda")
+        for _ in range(reps):
+            smp = s.draw(N + 1)[0]
+            for k in range(N):
+                counts[k] += torch.bincount(smp[k], minlength=I)
+        emp = counts.cpu().numpy() / (reps * Jd)
+        for k in range(N):
+            Mk = pinv.copy()
+            for m in range(N):
+                if m != k:
+                    Mk = Mk * G[m]
+            p = np.einsum("ia,ab,ib->i", U[k], Mk, U[k])
+            p = p / p.sum()
+            tv = 0.5 * np.abs(emp[k] - p).sum()
+            noise = 0.5 * np.sum(np.sqrt(2 * p / (np.pi * reps * Jd)))
+            assert tv <= 1.5 * noise + 1e-4, (precision, k, tv, noise)
 
 
 def test_philox_stream_equals_injected_oracle_uniforms(ftl):
