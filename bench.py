@@ -370,7 +370,11 @@ def run_ours(args, ws, rank, local):
         ms = max_over_ranks(e0.elapsed_time(e1) / steps, ws, dev)
         return ms, max_over_ranks(kms, ws, dev), clk
 
-    s = ftl.Sampler(U, J, R, "efficient", precision=args.precision, seed=seeds["sampler"])
+    s = ftl.Sampler(U, J, R, "efficient", precision=args.precision, seed=seeds["sampler"], autotune=False)
+    # the autotuner times the draw variants on this workload (set-up, outside
+    # the timed region) and selects the fastest for the timed draws
+    from fast_tensor_leverage_gb300 import autotune as AT
+    tuning = AT.tune_draw(s, store=False)
     clocks = ClockSampler(local) if rank == 0 else None
     ms, kernel_ms, clk = time_draws(s, args.steps, args.warmup, clocks)
     value = whole_job_rate(ws, J, ms / 1e3)
@@ -477,6 +481,9 @@ def run_ours(args, ws, rank, local):
         "clocks": clk,
         "cpu_baseline": cpu,
         "one_mode_excluded": one_excluded,
+        "autotune": {"family": "draw", "variant": tuning["variant"],
+                     "samples_per_warp": tuning["variant"] + 1 if tuning["ms"] else 1,
+                     "descent_ms_by_variant": {str(k): v for k, v in tuning["ms"].items()}},
         "accuracy": acc,
     }
     if fp64 is not None:

@@ -115,6 +115,9 @@ SIGNATURES = {
     "ftl_factor_shadow": ([_P, _I64, _P, _P], _INT),
     "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),
     "ftl_tree_bytes": ([_I64, _I64, _INT, _INT, _SZP], _INT),
+    "ftl_tune_variants": ([_INT, _INT, _INT, ctypes.POINTER(_INT), ctypes.POINTER(_INT)], _INT),
+    "ftl_tune_set": ([_INT, _INT, _INT, _INT], _INT),
+    "ftl_tune_get": ([_INT, _INT, _INT, ctypes.POINTER(_INT)], _INT),
     "ftl_node_layout": ([_INT, _INT, ctypes.POINTER(_INT), ctypes.POINTER(_INT), _P], _INT),
     "ftl_tree_build": ([_P, _I64, _INT, _I64, _INT, _P, _P], _INT),
     "ftl_tree_build_ex": ([_P, _I64, _INT, _I64, _INT, _P, _P, _P], _INT),

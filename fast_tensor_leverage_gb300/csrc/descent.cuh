@@ -50,14 +50,11 @@
 #ifndef FTL_DESC_RESIDENT_F64
 #define FTL_DESC_RESIDENT_F64 512
 #endif
-#ifndef FTL_DESC_CHAINS_D32
-#define FTL_DESC_CHAINS_D32 3      // FP32 DIAG32 draws: samples one warp descends in lockstep
-#endif
 #ifndef FTL_DESC_WARPS_D32
-#define FTL_DESC_WARPS_D32 4       // FP32 DIAG32 draws: warps per block
+#define FTL_DESC_WARPS_D32 4       // FP32 DIAG32 packed (multi-request) draws and tree sampler: warps per block
 #endif
 #ifndef FTL_DESC_RESIDENT_D32
-#define FTL_DESC_RESIDENT_D32 512  // FP32 DIAG32 draws: threads per SM the register budget is set for (128)
+#define FTL_DESC_RESIDENT_D32 512  // the same kernels: threads per SM the register budget is set for (128)
 #endif
 
 namespace ftl {

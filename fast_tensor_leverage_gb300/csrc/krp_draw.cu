@@ -16,6 +16,7 @@
 namespace ftl {
 
 int computem_launch(const ftl_krp_plan *plan, uint32_t j_norm, cudaStream_t st);
+int tuned_variant(int family, int R, int prec);
 
 struct DrawParams {
     int N, R, P, S;
@@ -285,20 +286,34 @@ __device__ __forceinline__ void draw_samples_d32(const DrawParams &p, int64_t i0
 }
 
 template <int RMAX, typename T, bool S32, bool DIAG>
-__global__ void __launch_bounds__(Blk<RMAX, T, DIAG>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T, DIAG>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
-    constexpr int WARPS = Blk<RMAX, T, DIAG>::WARPS;
+__global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T>::WARPS * 32)) krp_draw_kernel(DrawParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    DrawWarp<RMAX, T, DIAG> dw;
+    setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, p.R, p.P, p.S);
     const int warp = threadIdx.x >> 5;
-    if constexpr (DIAG && sizeof(T) == 4) {
-        constexpr int NC = FTL_DESC_CHAINS_D32;
-        for (int64_t i0 = ((int64_t)blockIdx.x * WARPS + warp) * NC; i0 < p.J; i0 += (int64_t)gridDim.x * WARPS * NC)
-            draw_samples_d32<S32, NC>(p, i0, threadIdx.x & 31);
-    } else {
-        extern __shared__ __align__(16) unsigned char smem_raw[];
-        DrawWarp<RMAX, T, DIAG> dw;
-        setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, p.R, p.P, p.S);
-        for (int64_t i = (int64_t)blockIdx.x * WARPS + warp; i < p.J; i += (int64_t)gridDim.x * WARPS)
-            draw_sample<RMAX, T, false, S32, DIAG>(p, i, dw);
-    }
+    for (int64_t i = (int64_t)blockIdx.x * Blk<RMAX, T>::WARPS + warp; i < p.J;
+         i += (int64_t)gridDim.x * Blk<RMAX, T>::WARPS)
+        draw_sample<RMAX, T, false, S32, DIAG>(p, i, dw);
+}
+
+// Block shape of the FP32 DIAG32 draw kernel per variant NC (samples a warp
+// descends in lockstep): warps per block and threads per SM its register
+// budget is set for.  NC = 1: 8 warps, 768 threads (85 registers); NC = 2
+// and 3: 4 warps, 512 threads (128 registers).  Which variant runs is the
+// autotuner's choice (ftl_tune_set), default NC = 3.
+template <int NC>
+struct D32Shape {
+    static constexpr int WARPS = NC == 1 ? 8 : 4;
+    static constexpr int RESIDENT = NC == 1 ? 768 : 512;
+};
+
+template <bool S32, int NC>
+__global__ void __launch_bounds__(D32Shape<NC>::WARPS * 32, D32Shape<NC>::RESIDENT / (D32Shape<NC>::WARPS * 32))
+    krp_draw_d32_kernel(DrawParams p) {
+    constexpr int WARPS = D32Shape<NC>::WARPS;
+    const int warp = threadIdx.x >> 5;
+    for (int64_t i0 = ((int64_t)blockIdx.x * WARPS + warp) * NC; i0 < p.J; i0 += (int64_t)gridDim.x * WARPS * NC)
+        draw_samples_d32<S32, NC>(p, i0, threadIdx.x & 31);
 }
 
 // Packed draw: the samples of up to FTL_MAX_PACK requests of the same rank
@@ -485,20 +500,32 @@ struct FastD32 {
     static constexpr bool value = DIAG && sizeof(T) == 4;
 };
 
+template <bool S32, int NC>
+static void launch_d32(const DrawParams &p, cudaStream_t st) {
+    constexpr int W = D32Shape<NC>::WARPS;
+    int64_t blocks = (p.J + (int64_t)W * NC - 1) / ((int64_t)W * NC);
+    blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
+    krp_draw_d32_kernel<S32, NC><<<(unsigned)blocks, W * 32, 0, st>>>(p);
+}
+
 template <int RMAX, typename T, bool S32, bool DIAG>
 static int launch_draw(const DrawParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T, DIAG>();
-    {
-        constexpr bool fast = FastD32<RMAX, T, DIAG>::value;
-        const int dwarps = Blk<RMAX, T, DIAG>::WARPS;
-        const int per_warp = fast ? FTL_DESC_CHAINS_D32 : 1;
-        const size_t dsmem = fast ? 0 : smem;
-        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32, DIAG>, dsmem, "krp_draw_kernel");
+    if constexpr (FastD32<RMAX, T, DIAG>::value) {
+        const int v = tuned_variant(FTL_TUNE_DRAW, p.R, FTL_PREC_FP32);
+        if (v == 0)
+            launch_d32<S32, 1>(p, st);
+        else if (v == 1)
+            launch_d32<S32, 2>(p, st);
+        else
+            launch_d32<S32, 3>(p, st);
+    } else {
+        const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32, DIAG>, smem, "krp_draw_kernel");
         if (arc) return arc;
-        int64_t blocks = (p.J + (int64_t)dwarps * per_warp - 1) / ((int64_t)dwarps * per_warp);
+        int64_t blocks = (p.J + warps - 1) / warps;
         blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-        krp_draw_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, dwarps * 32, dsmem, st>>>(p);
+        krp_draw_kernel<RMAX, T, S32, DIAG><<<(unsigned)blocks, warps * 32, smem, st>>>(p);
     }
     int rc = check_launch("krp_draw_kernel");
     if (rc || sizeof(T) == 8) return rc;

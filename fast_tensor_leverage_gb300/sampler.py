@@ -23,7 +23,7 @@ from . import _lib
 class Sampler:
     def __init__(self, U, J: int, R: int, type: str = "efficient", *, precision: str = "fp64",
                  seed: int | None = None, device=None, factor_shadows: bool = True,
-                 overlap_computem: bool = True):
+                 overlap_computem: bool = True, autotune="cached"):
         if type != "efficient":
             raise ValueError(
                 f"Unsupported argument {type!r} passed for sampler construction "
@@ -101,6 +101,17 @@ class Sampler:
         self._refresh_plan()
         for k in range(N):
             self.update_sampler(k)
+        # kernel variants: "cached" applies the autotuner's recorded choice
+        # for this GPU (if any); True also times the variants when there is
+        # none; False leaves the current selection
+        self.tuning = None
+        if autotune:
+            from . import autotune as AT
+            v = AT.apply_cached(R, self._prec, device=self.device)
+            if v is None and autotune is True:
+                self.tuning = AT.tune_draw(self)
+            else:
+                self.tuning = {"variant": v, "cached": v is not None}
 
     @staticmethod
     def _factor_input(u, R: int, name: str):

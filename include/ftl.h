@@ -495,6 +495,22 @@ int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_
                           double *const *weights_dev, const double *const *draws_dev,
                           const uint64_t *seeds, const uint64_t *ctrs, void *stream);
 
+/* ------------------------------------------------------------ tuning */
+
+/* Kernel variants: some kernels are compiled in several variants with the
+ * same results and different launch shapes.  The autotuner times them and
+ * records its choice for the current device; launches then use it.  No
+ * counterpart in the reference (its tuning knobs are compile flags).
+ *   ftl_tune_variants : number of variants of (family, R, prec) and the default
+ *   ftl_tune_set      : choose variant v (-1: the default) on the current device
+ *   ftl_tune_get      : the variant launches use now
+ * FTL_TUNE_DRAW: the FP32 draw on DIAG32 trees (16 < R <= 32); variant v
+ * descends v + 1 samples per warp in lockstep (default 2). */
+#define FTL_TUNE_DRAW 0
+int ftl_tune_variants(int family, int R, int prec, int *count, int *default_variant);
+int ftl_tune_set(int family, int R, int prec, int variant);
+int ftl_tune_get(int family, int R, int prec, int *variant);
+
 /* Fill out_dev[0..n) with the uniforms the in-kernel generator uses
  * (Philox4x32-10, key=seed, counter=ctr+i). */
 int ftl_philox_uniforms(double *out_dev, int64_t n, uint64_t seed, uint64_t ctr,
