@@ -66,6 +66,8 @@ def parse():
                     help="als: dims and nnz times this factor (a smaller case of the same kernels, for profiling)")
     ap.add_argument("--sweeps", type=int, default=20)
     ap.add_argument("--no-fp64-arm", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="sampling: skip the tree-build, CP-ALS and serving legs of the default line")
     return ap.parse_args()
 
 
@@ -443,6 +445,10 @@ def run_ours(args, ws, rank, local):
         del s
     if rank == 0:
         acc["small_krp_tv"] = {p: small_krp_tv(ftl, p) for p in ("fp32", "fp64")}
+    extras = {}
+    if not args.no_extras:
+        extras["tree_build"] = tree_build_rates(U[0], R, ("fp32", "tf32x3", "bf16"), reps=5)
+        extras["tree_build"]["shape"] = f"I={I}, R={R} (one factor of the workload)"
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -454,6 +460,13 @@ def run_ours(args, ws, rank, local):
         if par is not None:
             acc.update(par)
 
+    if not args.no_extras:
+        # CP-ALS at 1/6 of the C3 size (5 sweeps) and a short serving run at a
+        # sustainable rate, measured in the same process as the headline
+        extras["als"] = als_summary(dev, replica_seeds(rank)["sparse"], scale=0.167, sweeps=5,
+                                    cpu_sweeps=1 if rank == 0 else 0)
+        torch.cuda.empty_cache()
+        extras["serve"] = serve_summary(dev, replica_seeds(rank)["serve"], rate=8.0, duration=10.0)
     if rank != 0:
         return None
     line = {
@@ -489,6 +502,7 @@ def run_ours(args, ws, rank, local):
     if fp64 is not None:
         line["fp64_path"] = fp64
         line["mixed_vs_fp64"] = value / fp64["value"]
+    line.update(extras)
     return line
 
 
@@ -644,6 +658,123 @@ def run_tree(args, ws, rank, local):
     return {"metric": f"partition-tree build, I=2^{args.log2I}, R={R}", "unit": "ms", "value": res["fp32"]["ms"],
             "higher_is_better": False, "n_gpus": ws, "builds": res,
             "peak_hbm_gbs": measured_peak()[0], "data": "synthetic (seeded N(0,1), 1% rows x100)"}
+
+
+def als_summary(dev, seed, scale, sweeps, cpu_sweeps=1):
+    """Randomized CP-ALS on the synthetic sparse stand-in for amazon-reviews
+    at `scale` of its size (dims 4.8e6 x 1.8e6 x 1.8e6 and 1.5e8 nonzeros
+    times scale; Zipf(1.1) indices, log1p(lognormal) values; R = 25,
+    J = 2^16; factors from the range finder), `sweeps` sweeps with
+    mixed-precision and with FP64 sampling: update-only device s/sweep and
+    exact fits.  With cpu_sweeps, the CPU port of the same ALS (the oracle's
+    restatement of ALS::execute_ds_als_update over its C sampler, all host
+    cores) runs that many sweeps from the same initial factors: its s/sweep
+    is the CPU baseline."""
+    import torch
+    import fast_tensor_leverage_gb300 as ftl
+    from fast_tensor_leverage_gb300.synthetic import sparse_powerlaw_tensor
+    dims = [int(d * scale) for d in (4_800_000, 1_800_000, 1_800_000)]
+    R, J = 25, 1 << 16
+    idx, vals = sparse_powerlaw_tensor(dims, int(1.5e8 * scale), 1.1, seed=seed, device=dev)
+    sp = ftl.SparseTensor(idx, vals, "sort", dims=dims)
+    rhs = type("Rhs", (), {})()
+    rhs.ten = sp
+    out = {"dims": dims, "nnz": sp.nnz, "R": R, "J": J, "sweeps": sweeps}
+    init = None
+    # FP64 twice (sampler seeds 11 and 12): randomized ALS trajectories depend
+    # on the sample stream, so the FP64 seed-to-seed fit spread is the
+    # yardstick for the mixed-vs-FP64 fit gap
+    for prec, sseed in (("fp32", 11), ("fp64", 11), ("fp64_seed12", 12)):
+        lhs = ftl.PyLowRank(dims, R, seed=7, sync_host=False)
+        sp.execute_rrf(lhs.ten, seed=7)
+        if init is None:
+            init = ([u.cpu().numpy() for u in lhs.ten.U_dev], lhs.ten.sigma_dev.cpu().numpy())
+        als = ftl.ALS(lhs.ten, sp)
+        als.initialize_ds_als(J, "efficient", precision=prec[:4], seed=sseed)
+        fit0 = lhs.compute_exact_fit(rhs)
+        st = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(st)
+        for _ in range(sweeps):
+            for j in range(3):
+                als.execute_ds_als_update(j, True, True)
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        out[prec] = {"s_per_sweep": e0.elapsed_time(e1) / 1e3 / sweeps, "fit_initial": fit0,
+                     "fit_final": lhs.compute_exact_fit(rhs)}
+        del als, lhs
+        torch.cuda.empty_cache()
+    out["fit_gap_mixed_vs_fp64"] = out["fp32"]["fit_final"] - out["fp64"]["fit_final"]
+    out["fit_gap_fp64_seed_to_seed"] = out["fp64_seed12"]["fit_final"] - out["fp64"]["fit_final"]
+    if cpu_sweeps:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        # the port's per-mode lookups (nonzeros stably sorted by their fiber
+        # key over the other modes, as its constructor sorts them), sorted on
+        # the GPU to keep this leg short
+        lookups = []
+        for j in range(3):
+            key = torch.zeros(idx.shape[0], dtype=torch.int64, device=dev)
+            for k in range(3):
+                if k != j:
+                    key = key * dims[k] + idx[:, k].to(torch.int64)
+            ks, perm = torch.sort(key, stable=True)
+            lookups.append((ks.cpu().numpy().astype(np.uint64), idx[perm, j].to(torch.int64).cpu().numpy(),
+                            vals[perm].cpu().numpy()))
+            del key, ks, perm
+        idx_h = idx.cpu().numpy().astype(np.uint32)
+        vals_h = vals.cpu().numpy()
+        del idx, vals
+        t0 = time.perf_counter()
+        o = O.OracleALS(init[0], init[1], idx_h, vals_h, J, dims=dims, lookups=lookups)
+        t_setup = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctr = 0
+        for _ in range(cpu_sweeps):
+            for j in range(3):
+                o.update(j, O.philox_uniforms(11, ctr, 2 * 3 * J))
+                ctr += 2 * 3 * J
+        t = (time.perf_counter() - t0) / cpu_sweeps
+        out["cpu_baseline"] = {"s_per_sweep": t, "unit": "s/sweep", "cores": threads, "kind": "port",
+                               "sample": f"{cpu_sweeps} sweep(s) of the CPU port from the same initial factors "
+                                         f"(set-up {t_setup:.1f} s not counted)"}
+        out["mixed_vs_cpu"] = t / out["fp32"]["s_per_sweep"]
+    return out
+
+
+def serve_summary(dev, seed, rate, duration, max_active=32, budget_gb=160.0):
+    """A short Poisson stream of sampling and 5-sweep CP-ALS requests (the
+    serving mix: N 3..6, I 1e4..1e7, R 8..128, J 2^10..2^17) through the
+    serving engine; p50/p99 latency from scheduled arrival to results on the
+    host, and the completed rate."""
+    import torch
+    from fast_tensor_leverage_gb300 import serving as S
+    warm = S.ServingEngine(int(budget_gb * 1e9), max_active=4, device=dev)
+    for _, r in S.poisson_request_stream(99, 1000.0, 0.01, als_fraction=0.5, I_range=(1e4, 1e5),
+                                         J_log2_range=(10, 12), nnz_range=(1e5, 2e5)):
+        warm.submit(r, arrival=0.0)
+    while not warm.idle():
+        warm.tick()
+    del warm
+    torch.cuda.synchronize(dev)
+    torch.cuda.empty_cache()
+    stream = S.poisson_request_stream(seed, rate, duration, als_fraction=0.2)
+    for _, r in stream:
+        if isinstance(r, S.ALSRequest) and isinstance(r.idx, S.SyntheticSparse):
+            r.idx, r.vals = r.idx.materialize(dev)
+    torch.cuda.synchronize(dev)
+    eng = S.ServingEngine(int(budget_gb * 1e9), max_active=max_active, device=dev, reserve=True)
+    done = eng.run(stream)
+    torch.cuda.synchronize(dev)
+    makespan = max(h.done for h in done) - min(h.arrival for h in done)
+    tot = S.latency_stats(done)
+    samp = [h for h in done if isinstance(h.request, S.SampleRequest)]
+    als = [h for h in done if isinstance(h.request, S.ALSRequest)]
+    return {"offered_rate": rate, "duration_s": duration, "requests": len(stream), "completed": len(done),
+            "completed_rate": len(done) / makespan, "p50_ms": tot["p50_ms"], "p99_ms": tot["p99_ms"],
+            "sampling": S.latency_stats(samp), "als": S.latency_stats(als)}
 
 
 def run_als(args, ws, rank, local):

@@ -296,7 +296,7 @@ class OracleALS:
     over OracleKRPSampler, for a COO sparse tensor (SortIdxLookup semantics,
     cpp_ext/sort_lookup.hpp:69-132)."""
 
-    def __init__(self, U_list, sigma, idx, vals, J: int, dims=None, rhs=None):
+    def __init__(self, U_list, sigma, idx, vals, J: int, dims=None, rhs=None, lookups=None):
         self.U = [np.array(u, dtype=np.float64, copy=True) for u in U_list]
         self.N = len(self.U)
         self.R = self.U[0].shape[1]
@@ -310,6 +310,12 @@ class OracleALS:
             return
         self.idx = np.ascontiguousarray(idx, dtype=np.uint32)
         self.vals = np.asarray(vals, dtype=np.float64)
+        if lookups is not None:
+            # per mode (sorted fiber keys, their mode-j indices, their values),
+            # the stable sort below made elsewhere
+            self.lookups = [(np.asarray(k, dtype=np.uint64), np.asarray(i, dtype=np.int64),
+                             np.asarray(v, dtype=np.float64)) for k, i, v in lookups]
+            return
         for j in range(self.N):
             k = fiber_keys(self.idx, self.dims, j)
             perm = np.argsort(k, kind="stable")
