@@ -208,14 +208,17 @@ def algorithmic_bytes(samples, dims, R, J, N, j, prec_bytes, shadow=False):
     """Bytes one descent launch must move at minimum (each distinct node or
     leaf block read once): per included mode, distinct Gram-tree nodes read
     (root + left child of every internal node on a sampled path) x P x s_G,
-    distinct leaf blocks x rows x R x 8 (FP64 factor rows of the leaf scan;
+    (P = values per node in the tree's layout), distinct leaf blocks x rows x
+    R x 8 (FP64 factor rows of the leaf scan;
     x 4 when the scan reads the FP32 factor copies, plus distinct sampled
     rows x R x 8 for the FP64 rows that update h), the whole eigen tree
     (2R-1) x P x s_G and its R x R FP64 row table; plus the outputs
     (samples N x J x 8, h J x R x 8, weights J x 8)."""
     import torch
     from fast_tensor_leverage_gb300 import _lib
-    P = R * (R + 1) // 2
+    # values per node in the trees' layout (packed triangle, or the 544-value
+    # wrapped-diagonal node of FP32 trees at 16 < R <= 32)
+    P = _lib.node_layout(R, 0 if prec_bytes == 8 else 1)[1]
     total = 0
     for k in range(N):
         if k == j:
@@ -260,10 +263,10 @@ def source_tag() -> str:
 
 def read_traffic(precision):
     """DRAM bytes per C2 descent launch from the committed ncu summary
-    (profiles/krp_draw_kernel_<precision>_*.md, lines 'traffic_bytes_per_launch:'
+    (profiles/krp_draw*_<precision>_*.md, lines 'traffic_bytes_per_launch:'
     and 'source_tag:').  None when no summary matches the current sources."""
     tag = source_tag()
-    for f in sorted((REPO / "profiles").glob(f"krp_draw_kernel_{precision}_*.md")):
+    for f in sorted((REPO / "profiles").glob(f"krp_draw*_{precision}_*.md")):
         vals = {}
         for line in f.read_text().splitlines():
             for key in ("traffic_bytes_per_launch:", "source_tag:"):
@@ -487,7 +490,8 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": (4 if args.precision == "fp32" else 3) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                     "peak_kind": peak_kind, "kernel": "krp_draw_kernel",
+                     "peak_kind": peak_kind,
+                     "kernel": "krp_draw_d32_kernel" if args.precision != "fp64" and 16 < R <= 32 else "krp_draw_kernel",
                      "kernel_ms": kernel_ms, "kernel_ms_source": "mean of the descent launches in the timed loop "
                      "(krp_draw_kernel + its fix-up pass), CUDA events on the launching stream",
                      "algorithmic_bytes_per_launch": alg},
