@@ -26,6 +26,11 @@
 #ifndef FTL_CM_MIXED_EIG_FP64
 #define FTL_CM_MIXED_EIG_FP64 0
 #endif
+// Mixed precision, R <= 32: the per-mode eigensolvers run in one warp
+// (one-sided Jacobi in registers) instead of the block-wide two-sided one.
+#ifndef FTL_CM_WARP_JACOBI
+#define FTL_CM_WARP_JACOBI 1
+#endif
 
 namespace ftl {
 
@@ -93,14 +98,20 @@ __global__ void computem_pinv_kernel(CMParams p) {
         __syncthreads();
         chol = cholesky_lower(A, R, 0.0, flag, cs + 1);
         if (chol) {
-            // V = L^-1 (lower), one column per thread, forward substitution
+            // V = L^-1 (lower), one column per thread, forward substitution;
+            // the diagonal reciprocals first, in parallel, so each column's
+            // dependent chain holds multiplications only (an FP64 division is
+            // a long dependent sequence on GB300's narrow FP64 pipe)
+            double *rdiag = cs + 2;  // R doubles of the cs scratch (R + 2 long), cs[0] is used below
+            for (int i = tid; i < R; i += nth) rdiag[i] = 1.0 / A[i * R + i];
+            __syncthreads();
             for (int jc = tid; jc < R; jc += nth) {
                 for (int i = 0; i < R; ++i) {
                     double y = 0.0;
                     if (i >= jc) {
                         double acc = (i == jc) ? 1.0 : 0.0;
                         for (int kk = jc; kk < i; ++kk) acc -= A[i * R + kk] * V[kk * R + jc];
-                        y = acc / A[i * R + i];
+                        y = acc * rdiag[i];
                     }
                     V[i * R + jc] = y;
                 }
@@ -190,8 +201,12 @@ __global__ void computem_pinv_kernel(CMParams p) {
     }
 }
 
+#ifndef FTL_CM_THREADS
+#define FTL_CM_THREADS 512
+#endif
+
 template <typename T>
-__global__ void computem_eig_kernel(CMParams p) {
+__global__ void __launch_bounds__(FTL_CM_THREADS) computem_eig_kernel(CMParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int R = p.R, RR = R * R, N = p.N, P = p.P, tid = threadIdx.x, nth = blockDim.x;
     const int k = blockIdx.x;
@@ -218,18 +233,38 @@ __global__ void computem_eig_kernel(CMParams p) {
         int *order32 = pq32 + R + 2;
         int *flag32 = order32 + R;
         const double *src = offset < N ? W : p.M;  // M[0] holds the full pseudo-inverse
-        for (int e = tid; e < RR; e += nth) A32[e] = (float)src[e];
+        // scale by 2^k (k even, exact) so the largest entry is near 1: the
+        // FP32 copy and its squares stay inside the FP32 range whatever the
+        // scale of the Grams (products of N Grams of 10^9-sized entries)
+        if (tid == 0) *flag32 = 0;
         __syncthreads();
-        jacobi_eigen<float>(A32, V32, R, cs32, pq32, flag32);
-        sort_ascending<float>(A32, R, order32);
-        for (int e = tid; e < RR; e += nth) {
-            int r = e / R, a = e - r * R;
-            int v = order32[r];
-            float lam = A32[v * R + v];
-            W[e] = (double)(sqrtf(fmaxf(lam, 0.0f)) * V32[a * R + v]);
+        int emax = 0;
+        for (int e = tid; e < RR; e += nth) emax = max(emax, (int)(((unsigned)__double2hiint(src[e]) >> 20) & 0x7ffu));
+        atomicMax(flag32, emax);
+        __syncthreads();
+        const int eb = *flag32;
+        int k = (eb >= 1 && eb <= 2045) ? 1023 - eb : 0;
+        k -= (k & 1);  // even: the square roots scale back exactly
+        __syncthreads();
+        const double sc = ldexp(1.0, k);
+        for (int e = tid; e < RR; e += nth) A32[e] = (float)(src[e] * sc);
+        __syncthreads();
+        if (R <= 32 && FTL_CM_WARP_JACOBI) {
+            // the PSD matrix by one warp (one-sided Jacobi in registers)
+            if (tid < 32) warp_jacobi_psd32(A32, R, k, W, p.lambda + (size_t)offset * R, tid);
+        } else {
+            jacobi_eigen<float>(A32, V32, R, cs32, pq32, flag32);
+            sort_ascending<float>(A32, R, order32);
+            const double wsc = ldexp(1.0, -k / 2), lsc = ldexp(1.0, -k);
+            for (int e = tid; e < RR; e += nth) {
+                int r = e / R, a = e - r * R;
+                int v = order32[r];
+                float lam = A32[v * R + v];
+                W[e] = (double)(sqrtf(fmaxf(lam, 0.0f)) * V32[a * R + v]) * wsc;
+            }
+            for (int r = tid; r < R; r += nth)
+                p.lambda[(size_t)offset * R + r] = (double)A32[order32[r] * R + order32[r]] * lsc;
         }
-        for (int r = tid; r < R; r += nth)
-            p.lambda[(size_t)offset * R + r] = (double)A32[order32[r] * R + order32[r]];
         __syncthreads();
     } else if (offset < N) {
         for (int e = tid; e < RR; e += nth) A[e] = W[e];

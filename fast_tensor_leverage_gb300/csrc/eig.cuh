@@ -12,6 +12,12 @@
 
 #include "ftl_common.cuh"
 
+// Stopping rule of the warp Jacobi: a pair is rotated while |a_p . a_q| >
+// FTL_CM_JACOBI_TOL 2^-24 |a_p| |a_q|.
+#ifndef FTL_CM_JACOBI_TOL
+#define FTL_CM_JACOBI_TOL 1.0f
+#endif
+
 namespace ftl {
 
 // In-place Jacobi on A (R x R, symmetric, row-major, element type T); V
@@ -148,6 +154,97 @@ __device__ void sort_ascending(const T *A, int R, int *order) {
         order[rank] = v;
     }
     __syncthreads();
+}
+
+// Eigendecomposition of a symmetric positive semidefinite R x R matrix
+// (R <= 32) by one warp, in FP32: the one-sided Jacobi method of Hestenes
+// ("Inversion of matrices by biorthogonalization", J. SIAM 6, 1958) on the
+// columns of A.  Lane j keeps column j of A (and of V, starting at the
+// identity) in registers; a round pairs the 32 columns by the round-robin
+// (circle) schedule -- lane 31 meets lane r in round r, lane l meets
+// (2r - l) mod 31 otherwise -- and each pair exchanges its columns with
+// shuffles, forms alpha = |a_p|^2, beta = |a_q|^2, gamma = a_p . a_q (both
+// lanes the same sums in the same order) and, unless |gamma| <= tol
+// sqrt(alpha beta), rotates [a_p a_q] (and [v_p v_q]) by the angle that
+// makes them orthogonal.  A sweep is 31 rounds; sweeps stop when one rotates
+// nothing.  Then A V has orthogonal columns A v_j = lambda_j v_j (A is PSD),
+// so lambda_j = |column j| and v_j = column j of V.  No block barrier: the
+// warp works alone.  Lanes past R hold zero columns and never rotate.
+//
+// Outputs (lane j < R writes its own entries): W[rank_j * R + a] =
+// sqrt(lambda_j) v_j[a] for a < R, rank_j the ascending rank of lambda_j
+// (a NaN ranks last, ties by index), and lam[rank_j] = lambda_j.
+//
+// A holds the matrix times 2^k (k even, chosen by the caller so that its
+// largest entry is near 1: the squared column norms stay inside the FP32
+// range); the outputs are scaled back: lambda 2^-k, W rows 2^(-k/2).
+__device__ inline void warp_jacobi_psd32(const float *A, int R, int k, double *W, double *lam, int lane) {
+    float a[32], v[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        a[i] = (i < R && lane < R) ? A[i * R + lane] : 0.0f;
+        v[i] = i == lane ? 1.0f : 0.0f;
+    }
+    const float tol = FTL_CM_JACOBI_TOL * 5.9604645e-08f;  // units of FP32 rounding
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        bool rotated = false;
+        for (int r = 0; r < 31; ++r) {
+            const int partner = lane == 31 ? r : (lane == r ? 31 : (2 * r - lane + 31) % 31);
+            float b[32];
+            float own = 0.0f, g = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                b[i] = __shfl_sync(0xffffffffu, a[i], partner);
+                own = fmaf(a[i], a[i], own);
+            }
+            const bool lo = lane < partner;
+            // gamma summed in the same order by both lanes: p's entry first
+#pragma unroll
+            for (int i = 0; i < 32; ++i) g = lo ? fmaf(a[i], b[i], g) : fmaf(b[i], a[i], g);
+            const float oth = __shfl_sync(0xffffffffu, own, partner);
+            const float ap = lo ? own : oth, aq = lo ? oth : own;
+            bool rot = g != 0.0f && fabsf(g) > tol * sqrtf(ap * aq);
+            float c = 1.0f, s = 0.0f;
+            if (rot) {
+                const float zeta = (aq - ap) / (2.0f * g);
+                const float t = (zeta >= 0.0f ? 1.0f : -1.0f) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                c = 1.0f / sqrtf(1.0f + t * t);
+                s = c * t;
+            }
+            rotated |= rot;
+            // p: c a_p - s a_q;  q: s a_p + c a_q  (both lanes of a pair
+            // rotate or neither: rot is computed from the same values)
+            const float cs_own = c, cs_oth = lo ? -s : s;
+            if (__any_sync(0xffffffffu, rot)) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float vb = __shfl_sync(0xffffffffu, v[i], partner);
+                    if (rot) {
+                        a[i] = fmaf(cs_own, a[i], cs_oth * b[i]);
+                        v[i] = fmaf(cs_own, v[i], cs_oth * vb);
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, rotated)) break;
+    }
+    float nrm = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) nrm = fmaf(a[i], a[i], nrm);
+    float lv = sqrtf(nrm);
+    if (lv != lv) lv = INFINITY;
+    int rank = 0;
+    for (int u = 0; u < R; ++u) {
+        const float lu = __shfl_sync(0xffffffffu, lv, u);
+        if (lu < lv || (lu == lv && u < lane)) ++rank;
+    }
+    if (lane < R) {
+        const double sq = (double)sqrtf(fmaxf(lv, 0.0f)) * ldexp(1.0, -k / 2);
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (i < R) W[rank * R + i] = sq * (double)v[i];
+        lam[rank] = (double)sqrtf(nrm) * ldexp(1.0, -k);
+    }
 }
 
 // In-place lower Cholesky factor of (A - shift I), A dense R x R FP64 in

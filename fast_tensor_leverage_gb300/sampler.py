@@ -303,4 +303,6 @@ class Sampler:
         return e[k][:, pos].copy()
 
     def workspace_M(self) -> np.ndarray:
-        return self.M.cpu().numpy().reshape(-1, self.R, self.R)
+        # the (2N+3) R x R slots; the status word and packed pseudo-inverse follow
+        RR = self.R * self.R
+        return self.M.cpu().numpy()[: (2 * self.N + 3) * RR].reshape(-1, self.R, self.R)

@@ -121,13 +121,13 @@ def c2_case(ftl):
     return {"N": N, "I": I, "R": R, "U": U, "U_host": U_host, "oracle": O.OracleKRPSampler(U_host, 4096, R)}
 
 
-@pytest.mark.parametrize("j,min_agree", [(4, 0.95), (0, 0.85)])
+@pytest.mark.parametrize("j,min_agree", [(4, 0.90), (0, 0.80)])
 def test_c2_scale_draw_matches_oracle(ftl, c2_case, j, min_agree):
     """At the benchmarked size (18-level Gram trees, I = 2^23): FP64 draws
     match the oracle index for index (except near-ties, oracle margin below
     NEAR_TIE), h bit-exact, weights within 1e-9.  Mixed-precision draws given
-    the same uniforms agree with the oracle's samples on >= 95% (j = N+1) /
-    85% (j = 0) of samples, with h bit-exact and weights within 1e-3 where
+    the same uniforms agree with the oracle's samples on >= 90% (j = N+1) /
+    80% (j = 0) of samples, with h bit-exact and weights within 1e-3 where
     they agree: FP32 forms place the 2^23 row boundaries of each mode's CDF
     about 1e-7 from their FP64 positions, and where per-mode eigenvalues
     cluster the FP32 eigenbasis differs inside the cluster, so the same
