@@ -14,6 +14,8 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "libftl_gb300.so"
 
 FTL_OK = 0
+FTL_E_TIMEOUT = 4
+FTL_E_CANCELLED = 5
 STATUS_NAMES = {
     1: "FTL_E_ARG",
     2: "FTL_E_OOM",
@@ -115,6 +117,7 @@ SIGNATURES = {
     "ftl_factor_shadow": ([_P, _I64, _P, _P], _INT),
     "ftl_tree_geometry": ([_I64, _I64, ctypes.POINTER(TreeGeom)], _INT),
     "ftl_tree_bytes": ([_I64, _I64, _INT, _INT, _SZP], _INT),
+    "ftl_krp_sample_packed_ctl": ([_P, _INT, _P, _P, _P, _P, _P, _P, _P, _P, _U64, _P, _P], _INT),
     "ftl_tune_variants": ([_INT, _INT, _INT, ctypes.POINTER(_INT), ctypes.POINTER(_INT)], _INT),
     "ftl_tune_set": ([_INT, _INT, _INT, _INT], _INT),
     "ftl_tune_get": ([_INT, _INT, _INT, ctypes.POINTER(_INT)], _INT),

@@ -324,7 +324,48 @@ struct MultiDrawParams {
     int n;
     int64_t cum[FTL_MAX_PACK + 1];
     DrawParams req[FTL_MAX_PACK];
+    // serving controls (ftl_krp_sample_packed_ctl); ctl == nullptr: none
+    ftl_pack_status *ctl;
+    const volatile uint32_t *cancel[FTL_MAX_PACK];  // per request, may be null
+    uint64_t budget_ns;                             // 0: no time budget
 };
+
+// Serving controls of a packed draw, checked by a warp before each sample:
+// a request whose cancel flag is set, or any request once the launch has run
+// longer than its budget (%globaltimer since the first warp started), has
+// its remaining samples skipped and its status set (first reason wins).  The
+// cancel flag (host-writable memory) is read every 8th sample a warp takes,
+// the timer every sample; `stopped` caches the requests this warp stopped.
+// Nothing waits: a stopped launch just finishes early.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool pack_stop(const MultiDrawParams &mp, int r, int &iter, unsigned &stopped, int lane) {
+    if (mp.ctl == nullptr) return false;
+    if (stopped & (1u << r)) return true;
+    uint32_t code = 0;
+    if (lane == 0) {
+        if (mp.cancel[r] && (iter & 7) == 0 && *mp.cancel[r] != 0u) code = FTL_E_CANCELLED;
+        if (!code && mp.budget_ns) {
+            unsigned long long *t0p = (unsigned long long *)&mp.ctl->start_ns;
+            const uint64_t now = global_ns();
+            unsigned long long t0 = *(volatile unsigned long long *)t0p;
+            if (t0 == 0ull) {
+                const unsigned long long prev = atomicCAS(t0p, 0ull, (unsigned long long)now);
+                t0 = prev == 0ull ? (unsigned long long)now : prev;
+            }
+            if (now - (uint64_t)t0 > mp.budget_ns) code = FTL_E_TIMEOUT;
+        }
+        if (code) atomicCAS((unsigned int *)&mp.ctl->status[r], 0u, code);
+    }
+    ++iter;
+    code = __shfl_sync(0xffffffffu, code, 0);
+    if (code) stopped |= 1u << r;
+    return code != 0;
+}
 
 template <int RMAX, typename T, bool S32, bool DIAG>
 __global__ void __launch_bounds__(Blk<RMAX, T, DIAG>::WARPS * 32, Resident<T, DIAG>::value / (Blk<RMAX, T, DIAG>::WARPS * 32)) krp_draw_multi_kernel(MultiDrawParams mp) {
@@ -335,18 +376,24 @@ __global__ void __launch_bounds__(Blk<RMAX, T, DIAG>::WARPS * 32, Resident<T, DI
         // one sample per warp (neighbouring samples may belong to different
         // requests, i.e. different trees); the same per-sample arithmetic as
         // krp_draw_kernel
+        int iter = 0;
+        unsigned stopped = 0u;
         for (int64_t g = (int64_t)blockIdx.x * WARPS + warp; g < total; g += (int64_t)gridDim.x * WARPS) {
             int r = 0;
             while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
+            if (pack_stop(mp, r, iter, stopped, threadIdx.x & 31)) continue;
             draw_samples_d32<S32, 1>(mp.req[r], g - mp.cum[r], threadIdx.x & 31);
         }
     } else {
         extern __shared__ __align__(16) unsigned char smem_raw[];
         DrawWarp<RMAX, T, DIAG> dw;
         setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
+        int iter = 0;
+        unsigned stopped = 0u;
         for (int64_t g = (int64_t)blockIdx.x * WARPS + warp; g < total; g += (int64_t)gridDim.x * WARPS) {
             int r = 0;
             while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
+            if (pack_stop(mp, r, iter, stopped, dw.lane)) continue;
             draw_sample<RMAX, T, false, S32, DIAG>(mp.req[r], g - mp.cum[r], dw);
         }
     }
@@ -395,7 +442,9 @@ __global__ void __launch_bounds__(Blk<RMAX, float>::WARPS * 32) krp_fixup_multi_
         const int64_t g = b + lane;
         int r = 0;
         while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
-        const bool bad = g < total && needs_redo<RMAX>(mp.req[r], g - mp.cum[r]);
+        // requests stopped by their controls are left as they are
+        const bool live = mp.ctl == nullptr || *(volatile uint32_t *)&mp.ctl->status[r] == 0u;
+        const bool bad = g < total && live && needs_redo<RMAX>(mp.req[r], g - mp.cum[r]);
         unsigned bal = __ballot_sync(0xffffffffu, bad);
         while (bal) {
             const int src = __ffs(bal) - 1;
@@ -721,14 +770,44 @@ static void fill_draw_params(DrawParams &p, const ftl_krp_plan *plan, uint32_t j
     p.ctr = ctr;
 }
 
+static int sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_t *js, uint64_t *const *samples,
+                         double *const *h, double *const *weights, const double *const *draws, const uint64_t *seeds,
+                         const uint64_t *ctrs, const uint32_t *const *cancel, uint64_t budget_ns,
+                         ftl_pack_status *status, void *stream);
+
 extern "C" int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_t *js,
                                      uint64_t *const *samples, double *const *h, double *const *weights,
                                      const double *const *draws, const uint64_t *seeds, const uint64_t *ctrs,
                                      void *stream) {
+    return sample_packed(plans, n, js, samples, h, weights, draws, seeds, ctrs, nullptr, 0, nullptr, stream);
+}
+
+extern "C" int ftl_krp_sample_packed_ctl(const ftl_krp_plan *const *plans, int n, const uint32_t *js,
+                                         uint64_t *const *samples, double *const *h, double *const *weights,
+                                         const double *const *draws, const uint64_t *seeds, const uint64_t *ctrs,
+                                         const uint32_t *const *cancel, uint64_t budget_ns, ftl_pack_status *status,
+                                         void *stream) {
+    FTL_CHECK_ARG(status != nullptr, "ftl_krp_sample_packed_ctl: status is NULL");
+    FTL_CHECK_ARG(((uintptr_t)status & 7u) == 0, "ftl_krp_sample_packed_ctl: status must be 8-byte aligned");
+    return sample_packed(plans, n, js, samples, h, weights, draws, seeds, ctrs, cancel, budget_ns, status, stream);
+}
+
+static int sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_t *js, uint64_t *const *samples,
+                         double *const *h, double *const *weights, const double *const *draws, const uint64_t *seeds,
+                         const uint64_t *ctrs, const uint32_t *const *cancel, uint64_t budget_ns,
+                         ftl_pack_status *status, void *stream) {
     FTL_CHECK_ARG(plans && js && samples && h && weights && seeds && ctrs, "ftl_krp_sample_packed: null array");
     FTL_CHECK_ARG(n >= 1 && n <= FTL_MAX_PACK, "ftl_krp_sample_packed: n=%d outside [1, %d]", n, FTL_MAX_PACK);
     MultiDrawParams mp;
     mp.n = n;
+    mp.ctl = status;
+    mp.budget_ns = budget_ns;
+    for (int i = 0; i < FTL_MAX_PACK; ++i) mp.cancel[i] = (cancel && i < n) ? cancel[i] : nullptr;
+    if (status) {
+        cudaError_t err = cudaMemsetAsync(status, 0, sizeof(ftl_pack_status), (cudaStream_t)stream);
+        if (err != cudaSuccess)
+            return fail(FTL_E_CUDA, "ftl_krp_sample_packed_ctl: clearing the status: %s", cudaGetErrorString(err));
+    }
     mp.cum[0] = 0;
     for (int i = 0; i < n; ++i) {
         int rc = validate_plan(plans[i]);

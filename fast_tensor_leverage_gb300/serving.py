@@ -86,6 +86,7 @@ class SampleRequest:
     j: int = 1 << 30
     precision: str = "fp32"
     seed: int = 0
+    budget_s: float = 0.0   # > 0: device-time budget of its draw (FTL_E_TIMEOUT past it)
 
 
 @dataclass
@@ -123,6 +124,17 @@ class Handle:
     _stage: str = "pending"
     _bypassed: int = 0
     _host: list = None
+    status: str = "ok"            # "ok", "cancelled" or "timeout" once done
+    _cancel: object = None        # pinned host flag the packed draw reads while it runs
+    _slot: int = 0                # index of the request in its packed launch
+
+    def cancel(self) -> None:
+        """Cancel the request: a pending one is dropped at the next tick, a
+        running draw stops at its next check of the flag (its status becomes
+        "cancelled"), a CP-ALS request issues no further sweep."""
+        if self._cancel is not None:
+            self._cancel[0] = 1
+        self.status = "cancelled" if self.done is None else self.status
 
     @property
     def latency(self) -> float | None:
@@ -162,6 +174,10 @@ def _factor_shapes(factors) -> tuple[list, int]:
     if isinstance(factors, GaussianFactors):
         return [int(I) for I in factors.dims], int(factors.R)
     return [int(f.shape[0]) for f in factors], int(factors[0].shape[1])
+
+
+# bytes of ftl_pack_status: the start time (8) and FTL_MAX_PACK statuses (4 each)
+_PACK_STATUS_BYTES = 8 + 4 * 16
 
 
 class ServingEngine:
@@ -210,6 +226,7 @@ class ServingEngine:
         if h.bytes > self.budget:
             raise ValueError(f"request {h.rid} needs {h.bytes} bytes, more than the whole budget {self.budget}")
         self._next += 1
+        h._cancel = torch.zeros(1, dtype=torch.int32, pin_memory=True)
         self.pending.append(h)
         return h
 
@@ -245,6 +262,12 @@ class ServingEngine:
 
     # ----------------------------------------------------------- internals
     def _admit(self) -> None:
+        # cancelled before admission: done without device work
+        for h in [h for h in self.pending if h.status == "cancelled"]:
+            self.pending.remove(h)
+            h.done = self.now()
+            h.result = {"status": "cancelled"}
+            self.finished.append(h)
         sizes = [h.bytes for h in self.pending]
         bypassed = [h._bypassed for h in self.pending]
         take = admission_order(sizes, bypassed, self.in_use, self.budget,
@@ -334,18 +357,29 @@ class ServingEngine:
                 ww = (ctypes.c_void_p * n)(*[h._obj.weights_dev.data_ptr() for h in chunk])
                 seeds = (ctypes.c_uint64 * n)(*[h._obj.seed for h in chunk])
                 ctrs = (ctypes.c_uint64 * n)(*[h._obj.counter for h in chunk])
-                _lib.call("ftl_krp_sample_packed", plans, n, js, smp, hh, ww, None, seeds, ctrs,
-                          int(ps.cuda_stream))
+                # serving controls: every request's cancel flag, and the
+                # launch's time budget = the tightest request budget
+                cancel = (ctypes.c_void_p * n)(*[h._cancel.data_ptr() for h in chunk])
+                budgets = [h.request.budget_s for h in chunk if h.request.budget_s > 0]
+                budget_ns = int(min(budgets) * 1e9) if budgets else 0
+                with torch.cuda.stream(ps):
+                    status = torch.empty(_PACK_STATUS_BYTES, dtype=torch.uint8, device=self.device)
+                _lib.call("ftl_krp_sample_packed_ctl", plans, n, js, smp, hh, ww, None, seeds, ctrs,
+                          cancel, budget_ns, status.data_ptr(), int(ps.cuda_stream))
                 self.packed_launches += 1
                 # results to pinned host buffers on the same stream: completion
                 # needs no host synchronisation
                 with torch.cuda.stream(ps):
-                    for h in chunk:
+                    st_host = torch.empty(_PACK_STATUS_BYTES, dtype=torch.uint8, pin_memory=True)
+                    st_host.copy_(status, non_blocking=True)
+                    for k, h in enumerate(chunk):
                         s: Sampler = h._obj
                         srcs = (s.samples_dev, s.h_dev, s.weights_dev)
                         h._host = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in srcs]
                         for dst, src in zip(h._host, srcs):
                             dst.copy_(src, non_blocking=True)
+                        h._host.append(st_host)
+                        h._slot = k
                 done = torch.cuda.Event()
                 done.record(ps)
                 for h in chunk:
@@ -358,6 +392,15 @@ class ServingEngine:
         req: ALSRequest = h.request
         if h._event is not None and not h._event.query():
             return  # previous sweep still on the device
+        if h._cancel is not None and int(h._cancel[0]) != 0:
+            # cancelled: no further sweep; retire once the last one is done
+            h.status = "cancelled"
+            h._host = None
+            h._stage = "running"
+            if h._event is None:
+                h._event = torch.cuda.Event()
+                h._event.record(h._stream)
+            return
         with torch.cuda.stream(h._stream):
             if h._sweeps_done == 0 or not self.graph_als:
                 for j in range(lr.N):
@@ -393,13 +436,22 @@ class ServingEngine:
 
     def _finish(self, h: Handle) -> None:
         # h._event covers the result copies: the pinned buffers are complete
-        if isinstance(h.request, SampleRequest):
-            samples, hh, w = (t.numpy() for t in h._host)
-            h.result = {"samples": samples.view(np.uint64), "h": hh, "weights": w}
+        if h._host is None:
+            h.result = {"status": h.status}
+        elif isinstance(h.request, SampleRequest):
+            samples, hh, w, st = h._host
+            code = int(st.numpy()[8:].view(np.uint32)[h._slot])
+            h.status = {0: "ok", _lib.FTL_E_CANCELLED: "cancelled", _lib.FTL_E_TIMEOUT: "timeout"}.get(code, "error")
+            if h.status == "ok":
+                h.result = {"samples": samples.numpy().view(np.uint64), "h": hh.numpy(), "weights": w.numpy(),
+                            "status": "ok"}
+            else:
+                h.result = {"status": h.status}  # the draw stopped early: no results
         else:
             terms, sigma, normsq = (t.numpy() for t in h._host[:3])
             resid = float(terms[0] + terms[1])
-            h.result = {"sigma": sigma, "fit": 1.0 - np.sqrt(max(resid, 0.0) / float(normsq[0]))}
+            h.status = "ok"  # every sweep ran (a cancel after the last one came too late)
+            h.result = {"sigma": sigma, "fit": 1.0 - np.sqrt(max(resid, 0.0) / float(normsq[0])), "status": "ok"}
             if h.request.return_factors:
                 h.result["U"] = [t.numpy() for t in h._host[3:]]
         h._host = None

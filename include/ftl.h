@@ -511,6 +511,33 @@ int ftl_tune_variants(int family, int R, int prec, int *count, int *default_vari
 int ftl_tune_set(int family, int R, int prec, int variant);
 int ftl_tune_get(int family, int R, int prec, int *variant);
 
+/* Status block of a controlled packed draw (device memory or host memory the
+ * device can access, 8-byte aligned); ftl_krp_sample_packed_ctl clears it on
+ * the stream before the launch.  No counterpart in the reference (it has no
+ * serving loop). */
+typedef struct ftl_pack_status {
+    uint64_t start_ns;               /* set by the launch (device global timer) */
+    uint32_t status[FTL_MAX_PACK];   /* per request: FTL_OK, FTL_E_CANCELLED or FTL_E_TIMEOUT */
+} ftl_pack_status;
+
+/* ftl_krp_sample_packed with serving controls.  cancel[i] (n pointers, the
+ * array or any entry may be NULL) points to a flag the host may set while
+ * the launch runs (pinned host memory or device memory): request i's
+ * remaining samples are then skipped and its status becomes
+ * FTL_E_CANCELLED.  budget_ns > 0: once the launch has run that long
+ * (device global timer), the remaining samples of every request are skipped
+ * and those requests get FTL_E_TIMEOUT.  A request with a non-zero status
+ * has incomplete results; the others are identical to ftl_krp_sample_packed.
+ * The kernel never waits on the flags: it reads them as it goes (the cancel
+ * flag about every 8 samples per warp) and finishes early.  Read the
+ * statuses after the stream reaches the end of the launch. */
+int ftl_krp_sample_packed_ctl(const ftl_krp_plan *const *plans, int n, const uint32_t *js,
+                              uint64_t *const *samples_dev, double *const *h_dev,
+                              double *const *weights_dev, const double *const *draws_dev,
+                              const uint64_t *seeds, const uint64_t *ctrs,
+                              const uint32_t *const *cancel, uint64_t budget_ns,
+                              ftl_pack_status *status, void *stream);
+
 /* Fill out_dev[0..n) with the uniforms the in-kernel generator uses
  * (Philox4x32-10, key=seed, counter=ctr+i). */
 int ftl_philox_uniforms(double *out_dev, int64_t n, uint64_t seed, uint64_t ctr,

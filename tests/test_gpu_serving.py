@@ -113,3 +113,83 @@ def test_captured_als_sweep_equals_eager(ftl):
         out.append([u.cpu().numpy() for u in lr.U_dev])
     for a, b in zip(*out):
         np.testing.assert_allclose(a, b, rtol=0, atol=1e-9 * np.abs(b).max())
+
+
+def _packed(ftl, samplers, js, cancel=None, budget_ns=0, ctl=True):
+    """One packed draw of the samplers through the C ABI (with or without
+    the serving controls); returns the statuses (or None)."""
+    import ctypes
+    from fast_tensor_leverage_gb300 import _lib
+    n = len(samplers)
+    plans = (ctypes.POINTER(_lib.KRPPlan) * n)(*[ctypes.pointer(s._plan) for s in samplers])
+    jj = (ctypes.c_uint32 * n)(*js)
+    smp = (ctypes.c_void_p * n)(*[s.samples_dev.data_ptr() for s in samplers])
+    hh = (ctypes.c_void_p * n)(*[s.h_dev.data_ptr() for s in samplers])
+    ww = (ctypes.c_void_p * n)(*[s.weights_dev.data_ptr() for s in samplers])
+    seeds = (ctypes.c_uint64 * n)(*[s.seed for s in samplers])
+    ctrs = (ctypes.c_uint64 * n)(*[0] * n)
+    st = torch.cuda.current_stream().cuda_stream
+    for s, j in zip(samplers, js):
+        _lib.call("ftl_krp_compute_m", ctypes.byref(s._plan), j, st)
+    if not ctl:
+        _lib.call("ftl_krp_sample_packed", plans, n, jj, smp, hh, ww, None, seeds, ctrs, st)
+        torch.cuda.synchronize()
+        return None
+    status = torch.zeros(72, dtype=torch.uint8, device="cuda")
+    flags = (ctypes.c_void_p * n)(*[(c.data_ptr() if c is not None else None) for c in (cancel or [None] * n)])
+    _lib.call("ftl_krp_sample_packed_ctl", plans, n, jj, smp, hh, ww, None, seeds, ctrs, flags, budget_ns,
+              status.data_ptr(), st)
+    torch.cuda.synchronize()
+    return status.cpu().numpy()[8:].view(np.uint32)[:n].tolist()
+
+
+def test_packed_draw_controls_cancel_and_timeout(ftl):
+    """Serving controls of the packed draw, without a GPU fault or wait:
+    a request whose host flag is set before the launch is skipped with
+    FTL_E_CANCELLED and leaves its outputs untouched while the other request
+    is bit-identical to the uncontrolled launch; a 1 ns budget stops every
+    request of a large launch with FTL_E_TIMEOUT; a generous budget changes
+    nothing."""
+    from fast_tensor_leverage_gb300 import _lib
+    rng = np.random.default_rng(44)
+    for R, prec in ((32, "fp32"), (16, "fp32"), (8, "fp64")):
+        U1 = [rng.normal(size=(3000, R)) for _ in range(3)]
+        U2 = [rng.normal(size=(2000, R)) for _ in range(3)]
+        a = ftl.Sampler(U1, 20000, R, "efficient", precision=prec, seed=1, overlap_computem=False)
+        b = ftl.Sampler(U2, 30000, R, "efficient", precision=prec, seed=2, overlap_computem=False)
+        _packed(ftl, [a, b], [4, 4], ctl=False)
+        ref_a = (a.samples_dev.clone(), a.h_dev.clone(), a.weights_dev.clone())
+        # cancelled before the launch
+        b.samples_dev.fill_(-7)
+        flag = torch.ones(1, dtype=torch.int32, pin_memory=True)
+        a.samples_dev.zero_()
+        st = _packed(ftl, [a, b], [4, 4], cancel=[None, flag])
+        assert st == [0, _lib.FTL_E_CANCELLED], (R, st)
+        assert torch.equal(a.samples_dev, ref_a[0]) and torch.equal(a.h_dev, ref_a[1])
+        assert torch.equal(a.weights_dev, ref_a[2])
+        assert bool((b.samples_dev == -7).all())
+        # a generous budget: nothing stops, results as without controls
+        st = _packed(ftl, [a, b], [4, 4], budget_ns=10**12)
+        assert st == [0, 0] and torch.equal(a.samples_dev, ref_a[0])
+        # 1 ns: every request times out
+        big = ftl.Sampler([rng.normal(size=(5000, R)) for _ in range(3)], 200000, R, "efficient", precision=prec,
+                          seed=3, overlap_computem=False)
+        st = _packed(ftl, [big, a], [4, 4], budget_ns=1)
+        assert st == [_lib.FTL_E_TIMEOUT, _lib.FTL_E_TIMEOUT], (R, st)
+
+
+def test_engine_cancel(ftl):
+    """ServingEngine.cancel: a request cancelled while pending finishes
+    with status "cancelled" and no device work; the others complete with
+    their results."""
+    from fast_tensor_leverage_gb300 import serving as S
+    rng = np.random.default_rng(3)
+    eng = S.ServingEngine(8 << 30, max_active=4)
+    hs = [eng.submit(S.SampleRequest([rng.normal(size=(1000, 8)) for _ in range(3)], 2000, 4, "fp32", seed=k))
+          for k in range(3)]
+    hs[1].cancel()
+    while not eng.idle():
+        eng.tick()
+    assert hs[1].status == "cancelled" and hs[1].result == {"status": "cancelled"}
+    for k in (0, 2):
+        assert hs[k].status == "ok" and hs[k].result["samples"].shape == (3, 2000)
