@@ -334,18 +334,25 @@ struct MultiDrawParams {
 // a request whose cancel flag is set, or any request once the launch has run
 // longer than its budget (%globaltimer since the first warp started), has
 // its remaining samples skipped and its status set (first reason wins).  The
-// cancel flag (host-writable memory) is read every 8th sample a warp takes,
-// the timer every sample; `stopped` caches the requests this warp stopped.
-// Nothing waits: a stopped launch just finishes early.
+// cancel flag (host-writable memory) is read on a warp's first sample of a
+// request and then every 8th sample, so a flag set before the launch stops
+// every sample of its request; the timer is read every sample.  `stopped`
+// caches the requests this warp stopped.  Nothing waits: a stopped launch
+// just finishes early.
 __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
 
-__device__ __forceinline__ bool pack_stop(const MultiDrawParams &mp, int r, int &iter, unsigned &stopped, int lane) {
+__device__ __forceinline__ bool pack_stop(const MultiDrawParams &mp, int r, int &iter, int &last_r,
+                                          unsigned &stopped, int lane) {
     if (mp.ctl == nullptr) return false;
     if (stopped & (1u << r)) return true;
+    if (r != last_r) {
+        last_r = r;
+        iter = 0;
+    }
     uint32_t code = 0;
     if (lane == 0) {
         if (mp.cancel[r] && (iter & 7) == 0 && *mp.cancel[r] != 0u) code = FTL_E_CANCELLED;
@@ -357,7 +364,8 @@ __device__ __forceinline__ bool pack_stop(const MultiDrawParams &mp, int r, int 
                 const unsigned long long prev = atomicCAS(t0p, 0ull, (unsigned long long)now);
                 t0 = prev == 0ull ? (unsigned long long)now : prev;
             }
-            if (now - (uint64_t)t0 > mp.budget_ns) code = FTL_E_TIMEOUT;
+            // another warp may have set t0 after this warp read `now`
+            if (now > (uint64_t)t0 && now - (uint64_t)t0 > mp.budget_ns) code = FTL_E_TIMEOUT;
         }
         if (code) atomicCAS((unsigned int *)&mp.ctl->status[r], 0u, code);
     }
@@ -376,24 +384,24 @@ __global__ void __launch_bounds__(Blk<RMAX, T, DIAG>::WARPS * 32, Resident<T, DI
         // one sample per warp (neighbouring samples may belong to different
         // requests, i.e. different trees); the same per-sample arithmetic as
         // krp_draw_kernel
-        int iter = 0;
+        int iter = 0, last_r = -1;
         unsigned stopped = 0u;
         for (int64_t g = (int64_t)blockIdx.x * WARPS + warp; g < total; g += (int64_t)gridDim.x * WARPS) {
             int r = 0;
             while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
-            if (pack_stop(mp, r, iter, stopped, threadIdx.x & 31)) continue;
+            if (pack_stop(mp, r, iter, last_r, stopped, threadIdx.x & 31)) continue;
             draw_samples_d32<S32, 1>(mp.req[r], g - mp.cum[r], threadIdx.x & 31);
         }
     } else {
         extern __shared__ __align__(16) unsigned char smem_raw[];
         DrawWarp<RMAX, T, DIAG> dw;
         setup_draw_warp<RMAX, T, DIAG>(dw, smem_raw, mp.req[0].R, mp.req[0].P, mp.req[0].S);
-        int iter = 0;
+        int iter = 0, last_r = -1;
         unsigned stopped = 0u;
         for (int64_t g = (int64_t)blockIdx.x * WARPS + warp; g < total; g += (int64_t)gridDim.x * WARPS) {
             int r = 0;
             while (r + 1 < mp.n && mp.cum[r + 1] <= g) ++r;
-            if (pack_stop(mp, r, iter, stopped, dw.lane)) continue;
+            if (pack_stop(mp, r, iter, last_r, stopped, dw.lane)) continue;
             draw_sample<RMAX, T, false, S32, DIAG>(mp.req[r], g - mp.cum[r], dw);
         }
     }

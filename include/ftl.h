@@ -529,7 +529,9 @@ typedef struct ftl_pack_status {
  * and those requests get FTL_E_TIMEOUT.  A request with a non-zero status
  * has incomplete results; the others are identical to ftl_krp_sample_packed.
  * The kernel never waits on the flags: it reads them as it goes (the cancel
- * flag about every 8 samples per warp) and finishes early.  Read the
+ * flag on a warp's first sample of the request and then every 8th) and
+ * finishes early; a flag set before the launch stops every sample of its
+ * request.  Read the
  * statuses after the stream reaches the end of the launch. */
 int ftl_krp_sample_packed_ctl(const ftl_krp_plan *const *plans, int n, const uint32_t *js,
                               uint64_t *const *samples_dev, double *const *h_dev,

@@ -193,3 +193,16 @@ def test_engine_cancel(ftl):
     assert hs[1].status == "cancelled" and hs[1].result == {"status": "cancelled"}
     for k in (0, 2):
         assert hs[k].status == "ok" and hs[k].result["samples"].shape == (3, 2000)
+
+
+def test_engine_request_budget_times_out(ftl):
+    """A request whose device-time budget (1 ns) is shorter than its draw
+    finishes with status "timeout" and no results."""
+    from fast_tensor_leverage_gb300 import serving as S
+    rng = np.random.default_rng(4)
+    eng = S.ServingEngine(8 << 30, max_active=4)
+    h = eng.submit(S.SampleRequest([rng.normal(size=(4000, 16)) for _ in range(3)], 300000, 9, "fp32", seed=1,
+                                   budget_s=1e-9))
+    while not eng.idle():
+        eng.tick()
+    assert h.status == "timeout" and h.result == {"status": "timeout"}
