@@ -441,13 +441,31 @@ def run_ours(args, ws, rank, local):
             "weights_rel_err_median": float(wrel.median()) if wrel.numel() else None,
             "note": "coupling: TV(mixed law, FP64 law) <= P(indices differ under shared uniforms)"}
         samples64_host = smp64.cpu().numpy().astype(np.uint64)
+        if not args.no_extras:
+            # the tensor-core tree precisions on the same workload and uniforms
+            per = {}
+            for tp in ("tf32x3", "bf16"):
+                st_ = ftl.Sampler(U, J, R, "efficient", precision=tp, seed=seeds["sampler"], overlap_computem=False)
+                smp_t, _, w_t = st_.draw(j, shared)
+                same_t = (smp_t == smp64).all(dim=0)
+                mism_t = int((~same_t).sum())
+                wrel_t = ((w_t - w64).abs() / w64.abs())[same_t]
+                per[tp] = {"index_agreement": 1.0 - mism_t / J, "mismatches": mism_t,
+                           "tv_upper_bound_95": binom_upper(mism_t, J),
+                           "weights_rel_err_max": float(wrel_t.max()) if wrel_t.numel() else None}
+                del st_, smp_t, w_t
+                torch.cuda.empty_cache()
+            per["fp32"] = {k: acc["mixed_vs_fp64_same_uniforms"][k]
+                           for k in ("index_agreement", "mismatches", "tv_upper_bound_95", "weights_rel_err_max")}
+            acc["tree_precisions_vs_fp64_same_uniforms"] = per
         del s64
         torch.cuda.empty_cache()
     else:
         samples64_host = None
         del s
     if rank == 0:
-        acc["small_krp_tv"] = {p: small_krp_tv(ftl, p) for p in ("fp32", "fp64")}
+        acc["small_krp_tv"] = {p: small_krp_tv(ftl, p) for p in
+                               (("fp32", "fp64") if args.no_extras else ("fp32", "tf32x3", "bf16", "fp64"))}
     extras = {}
     if not args.no_extras:
         extras["tree_build"] = tree_build_rates(U[0], R, ("fp32", "tf32x3", "bf16"), reps=5)
@@ -499,7 +517,8 @@ def run_ours(args, ws, rank, local):
         "cpu_baseline": cpu,
         "one_mode_excluded": one_excluded,
         "autotune": {"family": "draw", "variant": tuning["variant"],
-                     "samples_per_warp": tuning["variant"] + 1 if tuning["ms"] else 1,
+                     "samples_per_warp": (1, 2, 3, 3, 4, 6)[tuning["variant"]] if tuning["ms"] else 1,
+                     "weights_in_shared_memory": bool(tuning["ms"]) and tuning["variant"] >= 3,
                      "descent_ms_by_variant": {str(k): v for k, v in tuning["ms"].items()}},
         "accuracy": acc,
     }

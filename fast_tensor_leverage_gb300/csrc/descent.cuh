@@ -314,6 +314,68 @@ struct QFormD32 {
     }
 };
 
+// QFormD32 with the 17 query weights of each lane kept in shared memory
+// instead of registers (a per-sample slot of 544 floats: four [lane] rows of
+// float4 for d = 0..15, then one [lane] row for d = 16; every lane reads and
+// writes only its own entries, so no synchronisation is needed).  Frees 17
+// registers per sample in flight; the same products in the same order as
+// QFormD32, so the same results bit for bit.
+struct QFormD32S {
+    float4 *w4;
+    float *w16;
+
+    __device__ __forceinline__ void bind(float *slot) {
+        w4 = reinterpret_cast<float4 *>(slot);
+        w16 = slot + 512;
+    }
+
+    __device__ __forceinline__ void setup_reg(float xa, int lane) {
+        float xx[17];
+        xx[0] = xa * xa;
+#pragma unroll
+        for (int d = 1; d < 16; ++d) xx[d] = (xa + xa) * __shfl_sync(0xffffffffu, xa, (lane + d) & 31);
+        xx[16] = xa * __shfl_sync(0xffffffffu, xa, (lane + 16) & 31);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w4[32 * q + lane] = make_float4(xx[4 * q], xx[4 * q + 1], xx[4 * q + 2], xx[4 * q + 3]);
+        w16[lane] = xx[16];
+    }
+
+    __device__ __forceinline__ float dot(const float4 (&g)[4], float g16) const {
+        const int lane = threadIdx.x & 31;
+        float4 x = w4[lane];
+        float a0 = g[0].x * x.x, a1 = g[0].y * x.y;
+        a0 = fmaf(g[0].z, x.z, a0);
+        a1 = fmaf(g[0].w, x.w, a1);
+        x = w4[32 + lane];
+        a0 = fmaf(g[1].x, x.x, a0);
+        a1 = fmaf(g[1].y, x.y, a1);
+        a0 = fmaf(g[1].z, x.z, a0);
+        a1 = fmaf(g[1].w, x.w, a1);
+        x = w4[64 + lane];
+        a0 = fmaf(g[2].x, x.x, a0);
+        a1 = fmaf(g[2].y, x.y, a1);
+        a0 = fmaf(g[2].z, x.z, a0);
+        a1 = fmaf(g[2].w, x.w, a1);
+        x = w4[96 + lane];
+        a0 = fmaf(g[3].x, x.x, a0);
+        a1 = fmaf(g[3].y, x.y, a1);
+        a0 = fmaf(g[3].z, x.z, a0);
+        a1 = fmaf(g[3].w, x.w, a1);
+        a0 = fmaf(g16, w16[lane], a0);
+        return a0 + a1;
+    }
+
+    __device__ __forceinline__ float partial(const float *__restrict__ node, int lane) const {
+        const float4 *v = reinterpret_cast<const float4 *>(node);
+        const float4 g[4] = {__ldg(v + lane), __ldg(v + 32 + lane), __ldg(v + 64 + lane), __ldg(v + 96 + lane)};
+        return dot(g, __ldg(node + 512 + lane));
+    }
+
+    __device__ __forceinline__ float eval(const float *__restrict__ node, int lane) const {
+        return warp_sum(partial(node, lane));
+    }
+};
+
 // The form type of a (rank bound, precision, layout).
 template <int RMAX, typename T, bool DIAG>
 struct QSel {
@@ -570,9 +632,9 @@ __device__ __forceinline__ int64_t descend_careful(const float *__restrict__ G, 
 // The decisions are descend_df's: t = draw * m_root in double-float, left
 // iff t <= m_left, a right turn subtracts m_left.  cu[c] receives the leaf,
 // frac[c] the leaf fraction, mroot[c] the root form.
-template <int NC>
+template <int NC, class QF>
 __device__ __forceinline__ void descend_d32_multi(const float *__restrict__ G, const DGeom &g, const float (&dh)[NC],
-                                                  const float (&dl)[NC], const QFormD32 (&qf)[NC], int lane,
+                                                  const float (&dl)[NC], const QF (&qf)[NC], int lane,
                                                   uint32_t (&cu)[NC], float (&frac)[NC], float (&mroot)[NC]) {
     constexpr int S = kDiag32Stride;
     if (is_leaf(g, 0)) {

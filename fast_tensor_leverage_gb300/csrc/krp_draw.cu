@@ -11,6 +11,8 @@
 // interchangeable.
 #include <algorithm>
 
+#include <type_traits>
+
 #include "descent.cuh"
 
 namespace ftl {
@@ -196,17 +198,18 @@ struct Resident {
 // h o W[u] and the h update.  Samples that meet a zero-mass block are
 // flagged for the careful redo as in draw_sample.  Each sample's arithmetic
 // does not depend on NC.
-template <bool S32, int NC>
-__device__ __forceinline__ void draw_samples_d32(const DrawParams &p, int64_t i0, int lane) {
+template <bool S32, int NC, bool SW = false>
+__device__ __forceinline__ void draw_samples_d32(const DrawParams &p, int64_t i0, int lane, float *slots = nullptr) {
     const int R = p.R, N = p.N;
     const size_t RR = (size_t)R * R;
     const float RJ = (float)((double)R / (double)p.J);
     const bool col = lane < R;
     float uh[NC], ul[NC];
     double h[NC];
-    QFormD32 qf[NC];
+    typename std::conditional<SW, QFormD32S, QFormD32>::type qf[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
+        if constexpr (SW) qf[c].bind(slots + c * kDiag32Stride);
         uh[c] = ul[c] = 0.0f;
         const int64_t i = i0 + c;
         if (lane < 2 * N && i < p.J) {
@@ -301,19 +304,21 @@ __global__ void __launch_bounds__(Blk<RMAX, T>::WARPS * 32, Resident<T, DIAG>::v
 // budget is set for.  NC = 1: 8 warps, 768 threads (85 registers); NC = 2
 // and 3: 4 warps, 512 threads (128 registers).  Which variant runs is the
 // autotuner's choice (ftl_tune_set), default NC = 3.
-template <int NC>
+template <int NC, bool SW = false>
 struct D32Shape {
     static constexpr int WARPS = NC == 1 ? 8 : 4;
-    static constexpr int RESIDENT = NC == 1 ? 768 : 512;
+    static constexpr int RESIDENT = SW ? (NC <= 3 ? 640 : NC == 4 ? 512 : 384) : (NC == 1 ? 768 : 512);
+    static constexpr size_t SMEM = SW ? (size_t)WARPS * NC * kDiag32Stride * sizeof(float) : 0;
 };
 
-template <bool S32, int NC>
-__global__ void __launch_bounds__(D32Shape<NC>::WARPS * 32, D32Shape<NC>::RESIDENT / (D32Shape<NC>::WARPS * 32))
+template <bool S32, int NC, bool SW>
+__global__ void __launch_bounds__(D32Shape<NC, SW>::WARPS * 32, D32Shape<NC, SW>::RESIDENT / (D32Shape<NC, SW>::WARPS * 32))
     krp_draw_d32_kernel(DrawParams p) {
-    constexpr int WARPS = D32Shape<NC>::WARPS;
+    constexpr int WARPS = D32Shape<NC, SW>::WARPS;
+    extern __shared__ __align__(16) float d32_slots[];
     const int warp = threadIdx.x >> 5;
     for (int64_t i0 = ((int64_t)blockIdx.x * WARPS + warp) * NC; i0 < p.J; i0 += (int64_t)gridDim.x * WARPS * NC)
-        draw_samples_d32<S32, NC>(p, i0, threadIdx.x & 31);
+        draw_samples_d32<S32, NC, SW>(p, i0, threadIdx.x & 31, SW ? d32_slots + warp * NC * kDiag32Stride : nullptr);
 }
 
 // Packed draw: the samples of up to FTL_MAX_PACK requests of the same rank
@@ -557,12 +562,16 @@ struct FastD32 {
     static constexpr bool value = DIAG && sizeof(T) == 4;
 };
 
-template <bool S32, int NC>
-static void launch_d32(const DrawParams &p, cudaStream_t st) {
-    constexpr int W = D32Shape<NC>::WARPS;
+template <bool S32, int NC, bool SW>
+static int launch_d32(const DrawParams &p, cudaStream_t st) {
+    using Sh = D32Shape<NC, SW>;
+    constexpr int W = Sh::WARPS;
+    const int arc = ensure_smem((const void *)krp_draw_d32_kernel<S32, NC, SW>, Sh::SMEM, "krp_draw_d32_kernel");
+    if (arc) return arc;
     int64_t blocks = (p.J + (int64_t)W * NC - 1) / ((int64_t)W * NC);
     blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)num_sms() * 64));
-    krp_draw_d32_kernel<S32, NC><<<(unsigned)blocks, W * 32, 0, st>>>(p);
+    krp_draw_d32_kernel<S32, NC, SW><<<(unsigned)blocks, W * 32, Sh::SMEM, st>>>(p);
+    return FTL_OK;
 }
 
 template <int RMAX, typename T, bool S32, bool DIAG>
@@ -570,13 +579,16 @@ static int launch_draw(const DrawParams &p, cudaStream_t st) {
     const int warps = Blk<RMAX, T>::WARPS;
     size_t smem = desc_smem<RMAX, T, DIAG>();
     if constexpr (FastD32<RMAX, T, DIAG>::value) {
-        const int v = tuned_variant(FTL_TUNE_DRAW, p.R, FTL_PREC_FP32);
-        if (v == 0)
-            launch_d32<S32, 1>(p, st);
-        else if (v == 1)
-            launch_d32<S32, 2>(p, st);
-        else
-            launch_d32<S32, 3>(p, st);
+        int lrc;
+        switch (tuned_variant(FTL_TUNE_DRAW, p.R, FTL_PREC_FP32)) {
+            case 0: lrc = launch_d32<S32, 1, false>(p, st); break;
+            case 1: lrc = launch_d32<S32, 2, false>(p, st); break;
+            case 3: lrc = launch_d32<S32, 3, true>(p, st); break;
+            case 4: lrc = launch_d32<S32, 4, true>(p, st); break;
+            case 5: lrc = launch_d32<S32, 6, true>(p, st); break;
+            default: lrc = launch_d32<S32, 3, false>(p, st); break;
+        }
+        if (lrc) return lrc;
     } else {
         const int arc = ensure_smem((const void *)krp_draw_kernel<RMAX, T, S32, DIAG>, smem, "krp_draw_kernel");
         if (arc) return arc;

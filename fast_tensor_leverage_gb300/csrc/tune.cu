@@ -9,10 +9,12 @@
 // class of the family.  Unset entries use the family's default.
 //
 // Families:
-//   FTL_TUNE_DRAW: the FP32 draw on DIAG32 trees (16 < R <= 32); variant v
-//     descends v + 1 samples per warp in lockstep (1: 8 warps per block,
-//     768 threads per SM; 2 and 3: 4 warps per block, 512 threads per SM).
-//     Other ranks and precisions have one variant.
+//   FTL_TUNE_DRAW: the FP32 draw on DIAG32 trees (16 < R <= 32); variants
+//     0, 1, 2 descend 1, 2, 3 samples per warp in lockstep with the query
+//     weights in registers (1: 8 warps per block, 768 threads per SM; 2 and
+//     3: 4 warps per block, 512 threads per SM); variants 3, 4, 5 keep the
+//     weights in shared memory and descend 3, 4, 6 samples per warp (640,
+//     512, 384 threads per SM).  Other ranks and precisions have one variant.
 #include <mutex>
 
 #include "ftl_common.cuh"
@@ -32,7 +34,7 @@ bool g_tune_init = false;
 int variant_class(int family, int R, int prec, int *count, int *dflt) {
     (void)family;
     if (storage_prec(prec) == FTL_PREC_FP32 && node_layout(R, 4) == FTL_LAYOUT_DIAG32) {
-        *count = 3;
+        *count = 6;
         *dflt = 2;
         return 1;
     }

@@ -504,8 +504,10 @@ int ftl_krp_sample_packed(const ftl_krp_plan *const *plans, int n, const uint32_
  *   ftl_tune_variants : number of variants of (family, R, prec) and the default
  *   ftl_tune_set      : choose variant v (-1: the default) on the current device
  *   ftl_tune_get      : the variant launches use now
- * FTL_TUNE_DRAW: the FP32 draw on DIAG32 trees (16 < R <= 32); variant v
- * descends v + 1 samples per warp in lockstep (default 2). */
+ * FTL_TUNE_DRAW: the FP32 draw on DIAG32 trees (16 < R <= 32); variants 0, 1,
+ * 2 descend 1, 2, 3 samples per warp in lockstep with the query weights in
+ * registers, variants 3, 4, 5 descend 3, 4, 6 with the weights in shared
+ * memory (default 2). */
 #define FTL_TUNE_DRAW 0
 int ftl_tune_variants(int family, int R, int prec, int *count, int *default_variant);
 int ftl_tune_set(int family, int R, int prec, int variant);

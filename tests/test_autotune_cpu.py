@@ -29,10 +29,10 @@ def test_choose_prefers_default_within_noise():
 
 
 def test_variant_table_through_the_c_abi():
-    # FP32 trees at 16 < R <= 32 have three draw variants, default 2
+    # FP32 trees at 16 < R <= 32 have six draw variants, default 2
     n, d = AT.variants(AT.FAMILY_DRAW, 32, _lib.PREC["fp32"])
-    assert (n, d) == (3, 2)
-    assert AT.variants(AT.FAMILY_DRAW, 25, _lib.PREC["tf32x3"]) == (3, 2)
+    assert (n, d) == (6, 2)
+    assert AT.variants(AT.FAMILY_DRAW, 25, _lib.PREC["tf32x3"]) == (6, 2)
     assert AT.variants(AT.FAMILY_DRAW, 64, _lib.PREC["fp32"]) == (1, 0)
     assert AT.variants(AT.FAMILY_DRAW, 32, _lib.PREC["fp64"]) == (1, 0)
     assert AT.get_variant(AT.FAMILY_DRAW, 32, 1) == 2
@@ -42,6 +42,6 @@ def test_variant_table_through_the_c_abi():
     AT.set_variant(AT.FAMILY_DRAW, 32, 1, -1)               # back to the default
     assert AT.get_variant(AT.FAMILY_DRAW, 32, 1) == 2
     with pytest.raises(_lib.FTLError):
-        AT.set_variant(AT.FAMILY_DRAW, 32, 1, 3)
+        AT.set_variant(AT.FAMILY_DRAW, 32, 1, 6)
     with pytest.raises(_lib.FTLError):
         AT.set_variant(7, 32, 1, 0)

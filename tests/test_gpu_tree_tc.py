@@ -58,6 +58,8 @@ def check_close(G, G64, R, tol):
     (7_777, 8, 8),
     (20, 32, 20),             # F = n < R: one leaf
     (1000, 24, 12),           # F < R
+    (8, 4, 4),                # R = 4: 32-byte rows, box taller than the factor
+    (1000, 4, 4),
 ])
 @pytest.mark.parametrize("precision", ["tf32x3", "bf16"])
 def test_tensor_core_tree_matches_fp64(ftl, n, R, F, precision):
