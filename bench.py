@@ -889,28 +889,38 @@ def run_lowrank(args, ws, rank, local):
     rhs = type("Rhs", (), {})()
     rhs.ten = rhs_ten
     out = {}
+    study = {}
+    precisions = ("fp64", "fp32", "tf32x3", "bf16")
     for R in (16, 64):
-        for prec in ("fp32", "fp64"):
+        for prec in precisions:
             lhs = ftl.PyLowRank(dims, R, seed=7, sync_host=False)
             lhs.ten.renormalize_columns(-1)
             als = ftl.ALS(lhs.ten, rhs_ten)
             als.initialize_ds_als(J, "efficient", precision=prec, seed=11)
-            fit0 = lhs.compute_exact_fit(rhs)
-            for j in range(4):   # one warm-up sweep (part of the run: fits include it)
-                als.execute_ds_als_update(j, True, True)
+            fits = [lhs.compute_exact_fit(rhs)]
             st = torch.cuda.current_stream(dev)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize(dev)
-            e0.record(st)
-            for _ in range(args.sweeps):
+            ms = 0.0
+            # sweep 0 is a warm-up (its fit is in the trace, its time is not);
+            # the fit after every sweep is computed outside the timed spans
+            for sweep in range(args.sweeps + 1):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
                 for j in range(4):
                     als.execute_ds_als_update(j, True, True)
-            e1.record(st)
-            torch.cuda.synchronize(dev)
-            out[f"R{R}_{prec}"] = {"s_per_sweep": e0.elapsed_time(e1) / 1e3 / args.sweeps, "fit_initial": fit0,
-                                   "fit_final": lhs.compute_exact_fit(rhs), "sweeps": args.sweeps + 1}
+                e1.record(st)
+                torch.cuda.synchronize(dev)
+                if sweep > 0:
+                    ms += e0.elapsed_time(e1)
+                fits.append(lhs.compute_exact_fit(rhs))
+            out[f"R{R}_{prec}"] = {"s_per_sweep": ms / 1e3 / args.sweeps, "fit_initial": fits[0],
+                                   "fit_final": fits[-1], "sweeps": args.sweeps + 1, "fit_trace": fits}
             del als, lhs
             torch.cuda.empty_cache()
+        ref = out[f"R{R}_fp64"]["fit_trace"]
+        study[f"R{R}"] = {p: {"max_abs_fit_diff_vs_fp64_per_sweep": max(abs(a - b) for a, b in
+                                                                      zip(out[f"R{R}_{p}"]["fit_trace"], ref)),
+                              "final_fit_diff_vs_fp64": out[f"R{R}_{p}"]["fit_final"] - ref[-1]}
+                          for p in precisions if p != "fp64"}
     if rank != 0:
         return None
     return {
@@ -918,7 +928,9 @@ def run_lowrank(args, ws, rank, local):
         out["R16_fp32"]["s_per_sweep"], "unit": "s/sweep", "higher_is_better": False, "n_gpus": ws,
         "dtype": "fp32 trees / fp64 solve", "data": "synthetic (seeded N(0,1) rank-16 factors, no noise)",
         "config": {"workload": "randomized CP-ALS of a low-rank tensor", "dims": dims, "true_rank": Rt, "J": J},
-        "runs": out,
+        "runs": out, "precision_study": study,
+        "note": "same initial factors and sampler seed per precision; fit_trace[s] = exact fit after sweep s "
+                "(s = 0: before the first); randomized trajectories differ once one sample differs",
     }
 
 

@@ -330,26 +330,41 @@ __global__ void pinv_square_kernel(const double *__restrict__ M, int R, int targ
             A[e] = a <= b ? M[e] : M[b * R + a];
         }
         __syncthreads();
-        if (cholesky_lower(A, R, 0.0, flag, cs + 1)) {
-            // X = L^-1 (lower), column c by forward substitution, into V
-            for (int c = tid; c < R; c += nth) {
-                for (int i = 0; i < c; ++i) V[i * R + c] = 0.0;
-                for (int i = c; i < R; ++i) {
-                    double t = (i == c) ? 1.0 : 0.0;
-                    for (int k = c; k < i; ++k) t -= A[i * R + k] * V[k * R + c];
-                    V[i * R + c] = t / A[i * R + i];
+        // small R: the inverse itself by the sweep operator (-M^-1 in the
+        // upper triangle); larger R: block-wide Cholesky factor, then column c
+        // of X = L^-1 by forward substitution, into V
+        const bool small = R <= 32 && nth * 2 >= R * (R + 1) / 2;
+        bool chol;
+        if (small) {
+            chol = sweep_inverse_spd(A, R, cs + 1, flag);
+        } else {
+            chol = cholesky_lower(A, R, 0.0, flag, cs + 1);
+            if (chol) {
+                for (int c = tid; c < R; c += nth) {
+                    for (int i = 0; i < c; ++i) V[i * R + c] = 0.0;
+                    for (int i = c; i < R; ++i) {
+                        double t = (i == c) ? 1.0 : 0.0;
+                        for (int k = c; k < i; ++k) t -= A[i * R + k] * V[k * R + c];
+                        V[i * R + c] = t / A[i * R + i];
+                    }
                 }
             }
             __syncthreads();
-            // out = X^T X; cs[0] accumulates ||out||_F^2
+        }
+        if (chol) {
+            // out = X^T X (or the swept inverse); cs[0] accumulates ||out||_F^2
             if (tid == 0) cs[0] = 0.0;
             __syncthreads();
             double fro = 0.0;
             for (int e = tid; e < RR; e += nth) {
                 int a = e / R, b = e - a * R;
-                const int k0 = a > b ? a : b;
                 double t = 0.0;
-                for (int k = k0; k < R; ++k) t += V[k * R + a] * V[k * R + b];
+                if (small) {
+                    t = -A[min(a, b) * R + max(a, b)];  // the swept upper triangle, mirrored
+                } else {
+                    const int k0 = a > b ? a : b;
+                    for (int k = k0; k < R; ++k) t += V[k * R + a] * V[k * R + b];
+                }
                 out[e] = t;
                 fro += t * t;
             }

@@ -88,45 +88,76 @@ __global__ void computem_pinv_kernel(CMParams p) {
     }
     double *status = p.M + cm_status_offset(N, R);  // 1.0: Cholesky path taken
     bool chol = false;
+    bool gj = false;  // A holds the swept matrix (sweep-operator path)
     if (p.prec == FTL_PREC_FP32 && !FTL_CM_MIXED_EIG_FP64) {
         // Mixed mode: when every eigenvalue of M[0] exceeds the reference's
-        // 1e-8 cut, its pseudo-inverse is the inverse, computed in FP64 from
-        // the Cholesky factor: pinv = L^-T L^-1.  The cut is certified by
-        // ||pinv||_F < 1 / (2e-8): lambda_min = 1 / ||M^-1||_2 >= 1 /
-        // ||M^-1||_F > 2e-8.  Otherwise the Jacobi path below runs.
+        // 1e-8 cut, its pseudo-inverse is the inverse, computed in FP64 by
+        // the sweep operator (R <= 32) or from the Cholesky factor, pinv
+        // = L^-T L^-1 (larger R).  The cut is certified by ||pinv||_F < 1 /
+        // (2e-8): lambda_min = 1 / ||M^-1||_2 >= 1 / ||M^-1||_F > 2e-8.
+        // Otherwise (or when a pivot is not positive) the Jacobi path below
+        // runs.
         for (int e = tid; e < RR; e += nth) A[e] = p.M[e];
         __syncthreads();
-        chol = cholesky_lower(A, R, 0.0, flag, cs + 1);
-        if (chol) {
-            // V = L^-1 (lower), one column per thread, forward substitution;
-            // the diagonal reciprocals first, in parallel, so each column's
-            // dependent chain holds multiplications only (an FP64 division is
-            // a long dependent sequence on GB300's narrow FP64 pipe)
-            double *rdiag = cs + 2;  // R doubles of the cs scratch (R + 2 long), cs[0] is used below
-            for (int i = tid; i < R; i += nth) rdiag[i] = 1.0 / A[i * R + i];
-            __syncthreads();
-            for (int jc = tid; jc < R; jc += nth) {
-                for (int i = 0; i < R; ++i) {
-                    double y = 0.0;
-                    if (i >= jc) {
-                        double acc = (i == jc) ? 1.0 : 0.0;
-                        for (int kk = jc; kk < i; ++kk) acc -= A[i * R + kk] * V[kk * R + jc];
-                        y = acc * rdiag[i];
+        double *rdiag = cs + 2;  // R doubles of the cs scratch (R + 2 long), cs[0] is used below
+        if (R <= 32 && nth * 2 >= R * (R + 1) / 2) {
+            // small R: the inverse itself by the sweep operator (upper
+            // triangle, -M^-1 on return; no triangular solve)
+            gj = true;
+            chol = sweep_inverse_spd(A, R, cs + 1, flag);
+        } else {
+            chol = cholesky_lower(A, R, 0.0, flag, cs + 1);
+            if (chol) {
+                // V = L^-1 (lower), one column per thread, forward substitution;
+                // the diagonal reciprocals first, in parallel, so each column's
+                // dependent chain holds multiplications only (an FP64 division is
+                // a long dependent sequence on GB300's narrow FP64 pipe)
+                for (int i = tid; i < R; i += nth) rdiag[i] = 1.0 / A[i * R + i];
+                __syncthreads();
+                for (int jc = tid; jc < R; jc += nth) {
+                    for (int i = 0; i < R; ++i) {
+                        double y = 0.0;
+                        if (i >= jc) {
+                            double acc = (i == jc) ? 1.0 : 0.0;
+                            for (int kk = jc; kk < i; ++kk) acc -= A[i * R + kk] * V[kk * R + jc];
+                            y = acc * rdiag[i];
+                        }
+                        V[i * R + jc] = y;
                     }
-                    V[i * R + jc] = y;
                 }
+                __syncthreads();
             }
-            __syncthreads();
+        }
+        if (chol) {
             if (tid == 0) cs[0] = 0.0;
             __syncthreads();
             double fro = 0.0;
-            for (int e = tid; e < RR; e += nth) {
-                int a = e / R, b = e - a * R;
-                int lo = max(a, b);
-                double acc = 0.0;
-                for (int kk = lo; kk < R; ++kk) acc += V[kk * R + a] * V[kk * R + b];
-                A[e] = acc;  // A is free again: the factor is no longer needed after this pass
-                fro += acc * acc;
+            if (gj) {
+                // M^-1 = minus the swept upper triangle, mirrored
+                double v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int e = tid + q * nth;
+                    v[q] = 0.0;
+                    if (e < RR) {
+                        const int a = e / R, b = e - a * R;
+                        v[q] = -A[min(a, b) * R + max(a, b)];
+                        fro += v[q] * v[q];
+                    }
+                }
+                __syncthreads();
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (tid + q * nth < RR) A[tid + q * nth] = v[q];
+            } else {
+                for (int e = tid; e < RR; e += nth) {
+                    int a = e / R, b = e - a * R;
+                    int lo = max(a, b);
+                    double acc = 0.0;
+                    for (int kk = lo; kk < R; ++kk) acc += V[kk * R + a] * V[kk * R + b];
+                    A[e] = acc;  // A is free again: the factor is no longer needed after this pass
+                    fro += acc * acc;
+                }
             }
             for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
             if ((tid & 31) == 0) atomicAdd(cs, fro);
@@ -285,6 +316,57 @@ __global__ void __launch_bounds__(FTL_CM_THREADS) computem_eig_kernel(CMParams p
     const int S = node_stride(R, sizeof(T));
     T *G = (T *)p.eig_G + (size_t)k * (2 * R - 1) * S;
     const DGeom g = p.eig;
+    if constexpr (sizeof(T) == 4) {
+        if (R <= 32) {
+            // FP32 trees, R <= 32: each thread owns node positions e and builds
+            // the whole tree at e in registers -- leaves (nodes R-1 .. 2R-2),
+            // then every internal node c = R-2 .. 0 as left + right (the same
+            // sums as level by level), then o root -- with no barrier and no
+            // re-reads of the tree.  Register indices are compile-time: the
+            // loops run over the 63 heap positions of R = 32 with predicates.
+            const T *root = (const T *)p.root[k];
+            // the eigenvector rows rounded to FP32 once, in shared memory (free
+            // again after the eigensolve): a conversion per use would run on
+            // the FP64 pipe
+            float *W32 = (float *)smem_raw;
+            __syncthreads();
+            for (int e = tid; e < RR; e += nth) W32[e] = (float)W[e];
+            __syncthreads();
+            for (int e = tid; e < S; e += nth) {
+                int a = 0, b = 0;
+                bool valid;
+                if (node_layout(R, 4) == FTL_LAYOUT_DIAG32) {
+                    diag32_entry(e, a, b);
+                    valid = a < R && b < R;
+                } else {
+                    valid = e < P;
+                    int rem = e;
+                    while (valid && rem >= R - a) {
+                        rem -= R - a;
+                        ++a;
+                    }
+                    b = a + rem;
+                }
+                T v[63];
+#pragma unroll
+                for (int c = 62; c >= 0; --c) {
+                    if (c >= 2 * R - 1) {
+                        v[c] = T(0);
+                    } else if (c >= R - 1) {
+                        const int u = (int)leaf_index(g, c);
+                        v[c] = valid ? W32[u * R + a] * W32[u * R + b] : T(0);
+                    } else {
+                        v[c] = v[c <= 30 ? 2 * c + 1 : 62] + v[c <= 30 ? 2 * c + 2 : 62];
+                    }
+                }
+                const T rt = root[e];
+#pragma unroll
+                for (int c = 0; c < 63; ++c)
+                    if (c < 2 * R - 1) G[c * S + e] = v[c] * rt;
+            }
+            return;
+        }
+    }
     // (an eigen tree has 2R - 1 <= 255 nodes of S <= 8256 values: 32-bit indexing)
     const int leaf_count = R;
     if (node_layout(R, sizeof(T)) == FTL_LAYOUT_DIAG32) {
