@@ -112,14 +112,8 @@ __host__ __device__ inline int packed_row_offset(int a, int R) { return a * R - 
 // (FTL_LAYOUT_PACKED and FTL_LAYOUT_DIAG32 are defined in ftl.h)
 constexpr int kDiag32Stride = 544;
 
-// Smallest R whose FP32 nodes use DIAG32 (17: every R above the 16 that the
-// packed layout's forms handle in registers).
-#ifndef FTL_DIAG32_MIN_R
-#define FTL_DIAG32_MIN_R 17
-#endif
-
 __host__ __device__ inline int node_layout(int R, int elem_bytes) {
-    return (elem_bytes == 4 && R >= FTL_DIAG32_MIN_R && R > 16 && R <= 32) ? FTL_LAYOUT_DIAG32 : FTL_LAYOUT_PACKED;
+    return (elem_bytes == 4 && R > 16 && R <= 32) ? FTL_LAYOUT_DIAG32 : FTL_LAYOUT_PACKED;
 }
 
 // Node stride in elements: every node starts 16-byte aligned and is read
