@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--als-scale", type=float, default=1.0,
                     help="als: dims and nnz times this factor (a smaller case of the same kernels, for profiling)")
     ap.add_argument("--sweeps", type=int, default=20)
+    ap.add_argument("--snr-db", type=lambda v: None if v.lower() == "none" else float(v), default=20.0,
+                    help="lowrank: signal-to-noise ratio of the counter-hash Gaussian noise (none: --snr-db none)")
     ap.add_argument("--no-fp64-arm", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="sampling: skip the tree-build, CP-ALS and serving legs of the default line")
@@ -886,6 +888,7 @@ def run_lowrank(args, ws, rank, local):
     dims, Rt, J = [65536] * 4, 16, 1 << 17
     rhs_ten = ftl.LowRankTensor(Rt, 10000, GaussianFactors(dims, Rt, seed=77 + rank).materialize(dev),
                                 sync_host=False)
+    noise_sigma = rhs_ten.set_noise_snr(args.snr_db, seed=91 + rank) if args.snr_db is not None else 0.0
     rhs = type("Rhs", (), {})()
     rhs.ten = rhs_ten
     out = {}
@@ -926,8 +929,13 @@ def run_lowrank(args, ws, rank, local):
     return {
         "metric": "CP-ALS s/sweep on a rank-16 low-rank tensor, 4 x 65536, J=2^17", "value":
         out["R16_fp32"]["s_per_sweep"], "unit": "s/sweep", "higher_is_better": False, "n_gpus": ws,
-        "dtype": "fp32 trees / fp64 solve", "data": "synthetic (seeded N(0,1) rank-16 factors, no noise)",
-        "config": {"workload": "randomized CP-ALS of a low-rank tensor", "dims": dims, "true_rank": Rt, "J": J},
+        "dtype": "fp32 trees / fp64 solve",
+        "data": "synthetic (seeded N(0,1) rank-16 factors" + (f", counter-hash Gaussian noise at SNR {args.snr_db} dB)"
+                                                          if args.snr_db is not None else ", no noise)"),
+        "config": {"workload": "randomized CP-ALS of a low-rank tensor", "dims": dims, "true_rank": Rt, "J": J,
+                   "snr_db": args.snr_db, "noise_sigma": noise_sigma,
+                   "fit_of_true_factors": (1.0 - float(np.sqrt(1.0 / (1.0 + 10.0 ** (args.snr_db / 10.0))))
+                                           if args.snr_db is not None else 1.0)},
         "runs": out, "precision_study": study,
         "note": "same initial factors and sampler seed per precision; fit_trace[s] = exact fit after sweep s "
                 "(s = 0: before the first); randomized trajectories differ once one sample differs",

@@ -108,6 +108,10 @@ SIGNATURES = {
     "ftl_dense_residual_workspace_bytes": ([_P], _INT),
     "ftl_dense_residual_terms": ([_P, _INT, _P, _INT, _P, _P, _INT, _P, ctypes.c_size_t, _P, _P], _INT),
     "ftl_lowrank_evaluate": ([_P, _INT, _INT, _P, _P, _INT, _I64, _P, _P], _INT),
+    "ftl_noise_sampled_mttkrp": ([_P, _INT, _INT, _U64, ctypes.c_double, _P, _I64, _P, _P, _P, _I64, _P, _P, _INT,
+                                  _P, _I64, _P], _INT),
+    "ftl_noise_add_at": ([_P, _INT, _U64, ctypes.c_double, _P, _INT, _I64, _P, _P], _INT),
+    "ftl_noise_add_fibers": ([_P, _INT, _U64, ctypes.c_double, _P, _I64, _INT, _P, _P], _INT),
     "ftl_lowrank_materialize": ([_P, _INT, _INT, _P, _P, _I64, _INT, _I64, _P, _P], _INT),
     "ftl_cross_gram_workspace_bytes": ([_INT, _INT, _P], _INT),
     "ftl_cross_gram": ([_P, _INT, _P, _INT, _I64, _P, ctypes.c_size_t, _P, _P], _INT),

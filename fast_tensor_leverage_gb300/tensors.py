@@ -94,6 +94,34 @@ class LowRankTensor:
         self._normsq = None
         if self.is_static:
             self._normsq = self._chain_sum_self()
+        # additive counter-hash Gaussian noise of the tensor as a right-hand
+        # side (set_noise); 0: none
+        self.noise_sigma = 0.0
+        self.noise_seed = 0
+        self._dims_c = (ctypes.c_int64 * self.N)(*self.dims)
+
+    def set_noise(self, sigma: float, seed: int = 0) -> None:
+        """Make this tensor, as a right-hand side, X + sigma Z with Z one
+        standard normal per entry, a function of the entry's index and
+        `seed` (ftl_noise_*: never stored).  Sampled MTTKRPs, evaluated
+        entries and materialised fibers include the noise; the norms and
+        residuals are their expectations over Z (the cross term with Z has
+        mean zero, the noise energy sigma^2 prod(dims) is added)."""
+        if sigma < 0:
+            raise ValueError("sigma must be >= 0")
+        self.noise_sigma = float(sigma)
+        self.noise_seed = int(seed)
+
+    def set_noise_snr(self, snr_db: float, seed: int = 0) -> float:
+        """set_noise with sigma for a signal-to-noise ratio of `snr_db`:
+        sigma^2 prod(dims) = ||[[sigma; U]]||^2 10^(-snr_db / 10).  Returns sigma."""
+        sig = float(np.sqrt(self._chain_sum_self() * 10.0 ** (-snr_db / 10.0) / float(np.prod(self.dims, dtype=np.float64))))
+        self.set_noise(sig, seed)
+        return sig
+
+    def noise_energy(self) -> float:
+        """sigma^2 prod(dims): the expected squared norm of the noise."""
+        return self.noise_sigma ** 2 * float(np.prod(self.dims, dtype=np.float64))
 
     # ---------------------------------------------------------- plumbing
     def _stream(self) -> int:
@@ -184,10 +212,11 @@ class LowRankTensor:
 
     def get_normsq(self) -> float:
         """||model||^2 = sum_rs sigma_r sigma_s prod_k (U_k^T U_k)_rs
-        (low_rank_tensor.hpp:70-76)."""
+        (low_rank_tensor.hpp:70-76), plus the expected noise energy when
+        set_noise is in effect."""
         if not self.is_static or self._normsq is None:
-            return self._chain_sum_self()
-        return self._normsq
+            return self._chain_sum_self() + self.noise_energy()
+        return self._normsq + self.noise_energy()
 
 
 # --------------------------------------------------- low-rank as a tensor
@@ -234,7 +263,8 @@ def _lr_compute_residual_normsq(self, sigma, U_list) -> float:
     t_other = _chain_sum(self._ws, st, Ud, Ro, sig, Ud, Ro, sig)
     t_cross = _chain_sum(self._ws, st, Ud, Ro, sig, self.U_dev, self.R, self.sigma_dev)
     v = torch.cat([t_self, t_other, t_cross]).cpu().numpy()
-    return max(float(v[0] + v[1] - 2.0 * v[2]), 0.0)
+    # with noise: plus its expected energy (the cross term with Z has mean 0)
+    return max(float(v[0] + v[1] - 2.0 * v[2]), 0.0) + self.noise_energy()
 
 
 def _lr_evaluate_indices(self, indices, result) -> None:
@@ -249,6 +279,9 @@ def _lr_evaluate_indices(self, indices, result) -> None:
     o = torch.empty(n, dtype=torch.float64, device=self.device)
     _lib.call("ftl_lowrank_evaluate", _ptrs(self.U_dev), self.N, self.R, self.sigma_dev.data_ptr(), idx_d.data_ptr(),
               0, n, o.data_ptr(), D.stream_ptr(self.device))
+    if self.noise_sigma:
+        _lib.call("ftl_noise_add_at", self._dims_c, self.N, self.noise_seed, self.noise_sigma, idx_d.data_ptr(), 0, n,
+                  o.data_ptr(), D.stream_ptr(self.device))
     out.reshape(-1)[:n] = o.cpu().numpy()
 
 
@@ -264,6 +297,9 @@ def _lr_materialize_rhs(self, samples, j: int, rhs_buf) -> None:
     o = torch.empty((n, cols), dtype=torch.float64, device=self.device)
     _lib.call("ftl_lowrank_materialize", _ptrs(self.U_dev), self.N, self.R, self.sigma_dev.data_ptr(), S_d.data_ptr(),
               n, j, self.dims[j] if j < self.N else 0, o.data_ptr(), D.stream_ptr(self.device))
+    if self.noise_sigma and j < self.N:
+        _lib.call("ftl_noise_add_fibers", self._dims_c, self.N, self.noise_seed, self.noise_sigma, S_d.data_ptr(), n,
+                  j, o.data_ptr(), D.stream_ptr(self.device))
     out.reshape(-1)[: n * cols] = o.cpu().numpy().reshape(-1)
 
 
@@ -272,6 +308,9 @@ def _lr_sampled_mttkrp_dev(self, samples, J, urep, ucnt, nuniq, w, h, R, j, out,
     ws = self._ws.get("lowrank_mttkrp", nb)
     _lib.call("ftl_lowrank_sampled_mttkrp", _ptrs(self.U_dev), self.sigma_dev.data_ptr(), self.N, self.R, j,
               samples, J, urep, ucnt, nuniq, J, w, h, R, ws.data_ptr(), nb, out, self.dims[j], out_rows, stream)
+    if self.noise_sigma:
+        _lib.call("ftl_noise_sampled_mttkrp", self._dims_c, self.N, j, self.noise_seed, self.noise_sigma, samples, J,
+                  urep, ucnt, nuniq, J, w, h, R, out, out_rows, stream)
 
 
 def _lr_execute_downsampled_mttkrp_py(self, samples, lhs, j: int, result) -> None:

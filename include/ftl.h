@@ -434,6 +434,27 @@ int ftl_lowrank_evaluate(const double *const *U, int N, int R, const double *sig
  * U_j^T (LowRankTensor::materialize_rhs, cpp_ext/low_rank_tensor.hpp:91-135). */
 int ftl_lowrank_materialize(const double *const *U, int N, int R, const double *sigma, const uint64_t *samples,
                             int64_t n, int j, int64_t I_j, double *out, void *stream);
+/* Counter-hash Gaussian noise on a black-box tensor of dims[N] (no
+ * counterpart in the reference): Z at the entry with linear (row-major) index
+ * L (mod 2^64) is the SplitMix64 finaliser of L * 0x9E3779B97F4A7C15 + seed,
+ * z, through Box-Muller in FP32: u1 = ((z >> 40) + 1) 2^-24, u2 = ((z >> 16)
+ * mod 2^24) 2^-24, Z = sqrt(-2 ln u1) cos(2 pi u2).  The noisy tensor is
+ * X + sigma Z; nothing is stored.
+ *   ftl_noise_sampled_mttkrp: out (rows 0..dims[j]-1, R columns) += sigma
+ *     sum_u coef_u Z(i, s_u) h[rep_u] over the unique samples, with the
+ *     arguments and coefficients of ftl_lowrank_sampled_mttkrp (FP32
+ *     accumulation over 512 samples, folded in FP64; deterministic)
+ *   ftl_noise_add_at: out[z] += sigma Z(idx_z) at n index tuples (n x N)
+ *   ftl_noise_add_fibers: out (n x dims[j]) += the noise fibers at n samples
+ *     (n x N uint64 row-major), mode j varying */
+int ftl_noise_sampled_mttkrp(const int64_t *dims, int N, int j, uint64_t seed, double sigma,
+                             const uint64_t *samples, int64_t J, const int32_t *urep, const int32_t *ucnt,
+                             const int64_t *num_unique_dev, int64_t num_unique, const double *w,
+                             const double *h, int R, double *out, int64_t out_rows, void *stream);
+int ftl_noise_add_at(const int64_t *dims, int N, uint64_t seed, double sigma, const void *idx, int idx_is_u64,
+                     int64_t n, double *out, void *stream);
+int ftl_noise_add_fibers(const int64_t *dims, int N, uint64_t seed, double sigma, const uint64_t *samples,
+                         int64_t n, int j, double *out, void *stream);
 /* out (out_rows x C) = X (I x K) M (K x C) in rows 0..I-1, zeros below
  * (the final product of LowRankTensor::execute_exact_mttkrp,
  * cpp_ext/low_rank_tensor.hpp:147-180). */
