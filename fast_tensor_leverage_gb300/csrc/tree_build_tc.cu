@@ -328,7 +328,10 @@ __global__ void __launch_bounds__(kThreads, 1) leaf_gram_tc_kernel(const __grid_
     for (int64_t i = 0; i < ntl; ++i) {
         const int s = (int)(i % kStages);
         const int b = (int)(i & 1);
-        const bool waited = mbar_wait(full + s, (uint32_t)((i / kStages) & 1), abort_flag);
+        // operand buffer b was last read by the MMA of tile i - 2: every warp
+        // waits for it (the epilogue warps already have) before overwriting it
+        bool waited = i < 2 || mbar_wait(mmad + b, (uint32_t)(((i - 2) >> 1) & 1), abort_flag);
+        waited = waited && mbar_wait(full + s, (uint32_t)((i / kStages) & 1), abort_flag);
         // convert: warp w = leaf w % 4 of the tile, rows 8 (w / 4) .. +7, lane = column
         if (waited) {
             const int lw = warp & 3, kg = warp >> 2;
