@@ -111,6 +111,8 @@ SIGNATURES = {
     "ftl_noise_sampled_mttkrp": ([_P, _INT, _INT, _U64, ctypes.c_double, _P, _I64, _P, _P, _P, _I64, _P, _P, _INT,
                                   _P, _I64, _P], _INT),
     "ftl_noise_add_at": ([_P, _INT, _U64, ctypes.c_double, _P, _INT, _I64, _P, _P], _INT),
+    "ftl_host_register": ([_P, ctypes.c_size_t, ctypes.POINTER(_INT)], _INT),
+    "ftl_host_unregister": ([_P], _INT),
     "ftl_noise_add_fibers": ([_P, _INT, _U64, ctypes.c_double, _P, _I64, _INT, _P, _P], _INT),
     "ftl_lowrank_materialize": ([_P, _INT, _INT, _P, _P, _I64, _INT, _I64, _P, _P], _INT),
     "ftl_cross_gram_workspace_bytes": ([_INT, _INT, _P], _INT),

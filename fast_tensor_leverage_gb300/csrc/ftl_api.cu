@@ -66,3 +66,25 @@ int num_sms() {
 extern "C" const char *ftl_last_error(void) { return ftl::g_last_error; }
 
 extern "C" int ftl_abi_version(void) { return 4; }
+
+extern "C" int ftl_host_register(void *ptr, size_t bytes, int *registered) {
+    FTL_CHECK_ARG(ptr && bytes > 0 && registered, "ftl_host_register: bad arguments");
+    *registered = 0;
+    const cudaError_t err = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (err == cudaSuccess) {
+        *registered = 1;
+        return FTL_OK;
+    }
+    (void)cudaGetLastError();  // a refused registration must not surface in a later error check
+    return FTL_OK;
+}
+
+extern "C" int ftl_host_unregister(void *ptr) {
+    FTL_CHECK_ARG(ptr, "ftl_host_unregister: NULL pointer");
+    const cudaError_t err = cudaHostUnregister(ptr);
+    if (err != cudaSuccess) {
+        (void)cudaGetLastError();
+        return ftl::fail(FTL_E_CUDA, "ftl_host_unregister: %s", cudaGetErrorString(err));
+    }
+    return FTL_OK;
+}

@@ -252,23 +252,26 @@ class Sampler:
     def _rows(self, j: int):
         return [k for k in range(self.N) if k != j]
 
-    def _copy_rows_out(self, j: int, s_out) -> None:
+    def _copy_rows_out(self, j: int, s_out) -> bool:
         # straight from the device into the caller's array (one copy; rows of
-        # excluded modes are left as they are, as in the reference)
+        # excluded modes are left as they are, as in the reference); returns
+        # whether a copy is still in flight (page-locked destination)
         N, J = self.N, self.J
         flat = s_out.reshape(-1)[: N * J].reshape(N, J).view(np.int64)
         if j >= N:
-            torch.from_numpy(flat).copy_(self.samples_dev)
-        else:
-            for k in self._rows(j):
-                torch.from_numpy(flat[k]).copy_(self.samples_dev[k])
+            return D.copy_to_numpy(flat, self.samples_dev)
+        pending = False
+        for k in self._rows(j):
+            pending |= D.copy_to_numpy(flat[k], self.samples_dev[k])
+        return pending
 
     def KRPDrawSamples(self, j: int, samples, draws=None) -> None:
         """Draw J samples from the KRP of all factors except j into
         samples (N x J uint64, row j untouched when j < N), in place."""
         s_out = D.require_numpy_out(samples, np.uint64, "samples", min_size=self.N * self.J)
         self.draw(j, draws)
-        self._copy_rows_out(int(j), s_out)
+        if self._copy_rows_out(int(j), s_out):
+            torch.cuda.current_stream(self.device).synchronize()
 
     def KRPDrawSamples_materialize(self, j: int, samples, h_out, weights_out, draws=None) -> None:
         """KRPDrawSamples plus copies of the sampled KRP rows h (J x R) and the
@@ -278,9 +281,14 @@ class Sampler:
         h_np = D.require_numpy_out(h_out, np.float64, "h_out", min_size=J * R)
         w_np = D.require_numpy_out(weights_out, np.float64, "weights_out", min_size=J)
         self.draw(j, draws)
-        self._copy_rows_out(int(j), s_out)
-        torch.from_numpy(h_np.reshape(-1)[: J * R]).copy_(self.h_dev.reshape(-1))
-        torch.from_numpy(w_np.reshape(-1)[:J]).copy_(self.weights_dev)
+        # results straight into the caller's arrays: DMA copies once the
+        # arrays are page-locked (registered on first use, released when they
+        # are garbage collected), then one wait for all of them
+        pending = self._copy_rows_out(int(j), s_out)
+        pending |= D.copy_to_numpy(h_np.reshape(-1)[: J * R], self.h_dev.reshape(-1))
+        pending |= D.copy_to_numpy(w_np.reshape(-1)[:J], self.weights_dev)
+        if pending:
+            torch.cuda.current_stream(self.device).synchronize()
 
     # ------------------------------------------------------- inspection
     @property

@@ -72,6 +72,15 @@ const char *ftl_last_error(void);
 /* ABI version, bumped on any signature change. */
 int ftl_abi_version(void);
 
+/* Page-lock a caller-owned host buffer (cudaHostRegister) so device results
+ * can be copied into it by DMA; *registered = 0 (and FTL_OK) when the runtime
+ * refuses (e.g. the pages are already registered), which callers treat as
+ * "stay pageable".  ftl_host_unregister must run before the buffer is
+ * freed.  No counterpart in the reference (its results are written by the
+ * CPU). */
+int ftl_host_register(void *ptr, size_t bytes, int *registered);
+int ftl_host_unregister(void *ptr);
+
 /* ---------------------------------------------------------------- trees */
 
 typedef struct ftl_tree_geom {
