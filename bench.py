@@ -499,7 +499,8 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": "exact KRP leverage sampling, N=3, I=2^23, R=32, J=50000, no mode excluded",
                    "N": N, "I": I, "R": R, "J": J, "j": j, "precision": args.precision,
                    "value_is": ("mixed precision (FP32 node Grams and forms, FP64 h, weights, pseudo-inverse): "
-                                "the north-star mixed-precision target; fp64_path is the reference's precision")
+                                "the mixed-precision mode this workload targets; fp64_path is the reference's "
+                                "precision")
                    if args.precision == "fp32" else "FP64 throughout (the reference's precision)",
                    "l2": "inputs larger than L2 (partition trees 3 x %.2f GB)" % (
                        (2 * (I // R) - 1) * (R * (R + 1) // 2) * prec_bytes / 1e9),
