@@ -345,19 +345,32 @@ __global__ void __launch_bounds__(kThreads, 1) leaf_gram_tc_kernel(const __grid_
             const int m = 32 * lw + c;
             unsigned char *op_hi = smem + kOffOp + (b * 2 + 0) * kOpBytes;
             unsigned char *op_lo = smem + kOffOp + (b * 2 + 1) * kOpBytes;
+            // full 32 x 32 leaf copied by the tensor map (the common case):
+            // no per-value bounds, copy or fallback checks
+            const bool full = p.use_tmap && R == 32 && F == 32 && rows_leaf == 32;
+            const double *srow = st + (lw * 32) * 32 + c;
+            float *u32 = (full && p.U32) ? p.U32 + row0 * 32 + (lw * 32) * 32 + c : nullptr;
 #pragma unroll
             for (int q = 2 * kg; q < 2 * kg + 2; ++q) {
                 float v[4];
+                if (full) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int k = 4 * q + j;
-                    double x = 0.0;
-                    if (c < R && k < rows_leaf) {
-                        const int e = (lw * F + k) * R + c;  // element of the staged tile
-                        x = ((uint32_t)e * 8u + 8u <= copied) ? st[e] : p.U[row0 * R + e];
+                    for (int j = 0; j < 4; ++j) {
+                        v[j] = d2f_rn(srow[(4 * q + j) * 32]);
+                        if (u32) u32[(4 * q + j) * 32] = v[j];
                     }
-                    v[j] = d2f_rn(x);
-                    if (p.U32 && c < R && k < rows_leaf) p.U32[row0 * R + (lw * F + k) * R + c] = v[j];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = 4 * q + j;
+                        double x = 0.0;
+                        if (c < R && k < rows_leaf) {
+                            const int e = (lw * F + k) * R + c;  // element of the staged tile
+                            x = ((uint32_t)e * 8u + 8u <= copied) ? st[e] : p.U[row0 * R + e];
+                        }
+                        v[j] = d2f_rn(x);
+                        if (p.U32 && c < R && k < rows_leaf) p.U32[row0 * R + (lw * F + k) * R + c] = v[j];
+                    }
                 }
                 if (MODE == 0) {
                     float4 h, l;
