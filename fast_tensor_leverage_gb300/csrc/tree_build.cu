@@ -59,16 +59,36 @@ __global__ void __launch_bounds__(256) leaf_gram_kernel(const double *__restrict
         const int64_t row0 = leaf0 * F;
         const int nrows = LB * (int)F;
         const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+        if (R == 32 && RP == 32 && ((uintptr_t)U & 15u) == 0 && ((uintptr_t)U32 & 7u) == 0) {
+            // 32 columns: a half warp per row, two columns per lane (16-byte
+            // loads, 8-byte copy stores): half the instructions per value
+            const int col = 2 * (lane & 15);
 #pragma unroll 4
-        for (int rr = threadIdx.x >> 5; rr < nrows; rr += nwarps) {
-            const int64_t row = row0 + rr;
-            for (int col = lane; col < RP; col += 32) {
-                T v = T(0);
-                if (row < n && col < R) {
-                    v = to_tree<T>(U[row * R + col]);
-                    if (sizeof(T) == 4 && U32) U32[row * R + col] = (float)v;  // the FP32 copy, same pass
+            for (int rr = 2 * (threadIdx.x >> 5) + (lane >> 4); rr < nrows; rr += 2 * nwarps) {
+                const int64_t row = row0 + rr;
+                T v0 = T(0), v1 = T(0);
+                if (row < n) {
+                    const double2 x = *reinterpret_cast<const double2 *>(U + row * 32 + col);
+                    v0 = to_tree<T>(x.x);
+                    v1 = to_tree<T>(x.y);
+                    if (sizeof(T) == 4 && U32)
+                        *reinterpret_cast<float2 *>(U32 + row * 32 + col) = make_float2((float)v0, (float)v1);
                 }
-                Us[rr * RP + col] = v;
+                Us[rr * 32 + col] = v0;
+                Us[rr * 32 + col + 1] = v1;
+            }
+        } else {
+#pragma unroll 4
+            for (int rr = threadIdx.x >> 5; rr < nrows; rr += nwarps) {
+                const int64_t row = row0 + rr;
+                for (int col = lane; col < RP; col += 32) {
+                    T v = T(0);
+                    if (row < n && col < R) {
+                        v = to_tree<T>(U[row * R + col]);
+                        if (sizeof(T) == 4 && U32) U32[row * R + col] = (float)v;  // the FP32 copy, same pass
+                    }
+                    Us[rr * RP + col] = v;
+                }
             }
         }
         __syncthreads();
