@@ -500,7 +500,7 @@ int ftl_gram_hadamard(const double *const *grams_dev, int N, int R, int exclude,
  * ftl_krp_draw, without workspaces: the eigen trees, computeM matrices,
  * eigenvalues and FP32 pseudo-inverse live in one static device array of
  * FTL_DRAW_STATIC_SCRATCH_BYTES that every GPU loading the library holds
- * until exit.  Configurations needing more (N x (2R-1) x P tree values plus
+ * until exit.  Configurations needing more (N x (2R-1) eigen-tree nodes plus
  * (2N+3) x R x R FP64, e.g. beyond N=16 at R=32) return FTL_E_ARG.  The
  * first call on a device looks up the array's address with that device
  * current; make it before any stream capture.  All calls share the array
